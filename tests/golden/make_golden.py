@@ -1,0 +1,175 @@
+"""Generate the golden fixtures by running the reference (Updes 1.0.3) itself.
+
+Usage (needs the Updes source tree; JAX is replaced by ``ref_shim``):
+
+    python tests/golden/make_golden.py /root/reference
+
+For every case in ``cases.CASES`` this builds the reference ``SquareCloud``
+(coordinates injected, so no RNG is shared), calls the reference's own
+``pde_solver_jit`` and its assembly functions (``assemble_op_Phi_P``,
+``assemble_bd_Phi_P``, ``assemble_A``, ``assemble_q``), and stores inputs and
+outputs in ``tests/golden/<case>.npz``.  It also differentiates the reference
+solve (reverse mode, through inv/GEMM/QR) for the boundary-control adjoint case.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+from functools import partial
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import ref_shim  # noqa: E402
+
+ref_shim.install()
+import torch  # noqa: E402
+
+import cases as C  # noqa: E402
+
+
+def load_reference(path):
+    sys.path.insert(0, path)
+    import updes  # noqa: F401
+    return updes
+
+
+def build(updes, case):
+    import jax.numpy as jnp
+    coords = C.grid_coords(case)
+
+    class InjectedCloud(updes.SquareCloud):
+        def define_node_coordinates(self, noise_key):
+            self.nodes = {g: torch.tensor(coords[g]) for g in range(self.N)}
+
+    cloud = InjectedCloud(Nx=case["Nx"], Ny=case["Ny"], facet_types=dict(case["facets"]),
+                          support_size="max")
+    kind, param = case["rbf"]
+    rbf = {"polyharmonic": lambda p: partial(updes.polyharmonic, a=int(p)),
+           "gaussian": lambda p: partial(updes.gaussian, eps=p),
+           "multiquadric": lambda p: partial(updes.multiquadric, eps=p),
+           "inverse_multiquadric": lambda p: partial(updes.inverse_multiquadric, eps=p),
+           "thin_plate": lambda p: partial(updes.thin_plate, a=int(p))}[kind](param)
+    op = case["op"]
+
+    def diff_operator(x, center=None, rbf=None, monomial=None, fields=None):
+        val = updes.nodal_value(x, center, rbf, monomial)
+        grad = updes.nodal_gradient(x, center, rbf, monomial)
+        lap = updes.nodal_laplacian(x, center, rbf, monomial)
+        if op == "laplacian":
+            return lap
+        if op == "advdiff":
+            return val / C.ADV_DT + jnp.dot(jnp.array(C.ADV_VEL), grad) - C.ADV_K * lap
+        if op == "kgrad":
+            return fields[0] * lap + fields[1] * grad[0] + fields[2] * grad[1]
+        if op == "darcy":
+            return updes.nodal_div_grad(x, center, rbf, monomial, (fields[0], fields[0])) + fields[1] * val
+        if op == "helmholtz_x":
+            return lap + (1.0 + x[0] * x[1]) * val
+        raise ValueError(op)
+
+    rhs = case["rhs"]
+
+    def rhs_operator(x, centers=None, rbf=None, fields=None):
+        if rhs == "value_over_dt":
+            return updes.value(x, fields[:, 0], centers, rbf) / C.ADV_DT
+        return C.FUNCS[rhs](jnp, x[0], x[1])
+
+    def bc_fn(name):
+        return lambda coord: C.FUNCS[name](jnp, coord[0], coord[1])
+
+    bcs = {}
+    for f, spec in case["bc"].items():
+        bcs[f] = (bc_fn(spec[0]), bc_fn(spec[1])) if isinstance(spec, tuple) else bc_fn(spec)
+    nodes = np.asarray(cloud.sorted_nodes)
+    fields = C.make_fields(case, nodes)
+    diff_args = None if fields is None else [torch.tensor(f) for f in fields]
+    rf = C.make_rhs_field(case, nodes)
+    rhs_args = None if rf is None else [torch.tensor(rf)]
+    return cloud, rbf, diff_operator, rhs_operator, bcs, diff_args, rhs_args
+
+
+def run_case(updes, name, case):
+    t0 = time.time()
+    cloud, rbf, dop, rop, bcs, diff_args, rhs_args = build(updes, case)
+    sol = updes.pde_solver_jit(diff_operator=dop, rhs_operator=rop, cloud=cloud, boundary_conditions=bcs,
+                               rbf=rbf, max_degree=case["max_degree"], diff_args=diff_args, rhs_args=rhs_args)
+    M = updes.compute_nb_monomials(case["max_degree"], 2)
+    bcs_arr = updes.boundary_conditions_func_to_arr(bcs, cloud)
+    robin, bcs2 = updes.duplicate_robin_coeffs(bcs_arr, cloud)
+    bcs2 = updes.zerofy_periodic_cond(bcs2, cloud)
+    opPhi, opP = updes.assemble_op_Phi_P(dop, cloud, rbf, M, diff_args)
+    bdPhi, bdP = updes.assemble_bd_Phi_P(cloud, rbf, M, robin)
+    A = updes.assemble_A(cloud, rbf, M)
+    q = updes.assemble_q(rop, bcs2, cloud, rbf, M, rhs_args)
+    npy = lambda t: np.asarray(t.detach() if isinstance(t, torch.Tensor) else t, dtype=np.float64)
+    diffMat = np.concatenate([np.concatenate([npy(opPhi), npy(opP)], 1),
+                              np.concatenate([npy(bdPhi), npy(bdP)], 1)], 0)
+    A = npy(A)
+    N = cloud.N
+    out = dict(
+        case=json.dumps(case),
+        coords=C.grid_coords(case),
+        sorted_nodes=npy(cloud.sorted_nodes),
+        counts=np.array([cloud.N, cloud.Ni, cloud.Nd, cloud.Nn, cloud.Nr, sum(cloud.Np)], np.int64),
+        facet_nodes=json.dumps({f: [int(i) for i in v] for f, v in cloud.facet_nodes.items()}),
+        sorted_outward_normals=npy(getattr(cloud, "sorted_outward_normals", torch.zeros(0, 2))),
+        robin=json.dumps({int(k): float(v) for k, v in robin.items()}),
+        q=npy(q), vals=npy(sol.vals), coeffs=npy(sol.coeffs),
+        diffMat_rowsum=diffMat.sum(1), diffMat_rowabs=np.abs(diffMat).sum(1),
+        A_rowsum=A.sum(1), A_rowabs=np.abs(A).sum(1),
+    )
+    if diff_args is not None:
+        out["fields"] = np.stack([npy(f) for f in diff_args])
+    if rhs_args is not None:
+        out["rhs_field"] = npy(rhs_args[0])
+    if N <= C.FULL_MATRIX_MAX_N:
+        out.update(diffMat=diffMat, A=A, B=npy(sol.mat))
+    else:
+        rows = np.arange(0, N, C.ROW_STRIDE)
+        out.update(diffMat_rows=rows, diffMat_sub=diffMat[rows], A_sub=A[rows],
+                   B_sub=npy(sol.mat)[rows])
+    # field operators on the solution (updes/operators.py:149-187)
+    out["grad_at_nodes"] = npy(updes.gradient_vec(cloud.sorted_nodes, sol.coeffs, cloud.sorted_nodes, rbf))
+    out["value_at_nodes"] = npy(updes.value_vec(cloud.sorted_nodes, sol.coeffs, cloud.sorted_nodes, rbf))
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: N={N} n={N + M} {time.time() - t0:.1f}s")
+
+
+def run_adjoint(updes):
+    """Reverse-mode gradient through the reference solve (inv → GEMM → QR → inv)."""
+    import jax.numpy as jnp
+    case = C.CASES[C.ADJOINT_CASE]
+    cloud, rbf, dop, rop, bcs, diff_args, rhs_args = build(updes, case)
+    north = cloud.facet_nodes["North"]
+    c0 = torch.tensor(C.adjoint_control(len(north)), requires_grad=True)
+    fields = [f.clone().requires_grad_(True) for f in diff_args]
+    nodes = cloud.sorted_nodes
+    ut = C.adjoint_target(jnp, nodes[:, 0], nodes[:, 1])
+    bcs = updes.boundary_conditions_func_to_arr(bcs, cloud)
+    bcs["North"] = c0
+    sol = updes.pde_solver(diff_operator=dop, rhs_operator=rop, cloud=cloud, boundary_conditions=bcs,
+                           rbf=rbf, max_degree=case["max_degree"], diff_args=fields, rhs_args=None)
+    Ni = cloud.Ni
+    J = torch.mean((sol.vals[:Ni] - ut[:Ni]) ** 2) + C.ADJOINT_REG * torch.sum(c0 ** 2)
+    J.backward()
+    np.savez_compressed(os.path.join(HERE, "adjoint_kgrad_10x10.npz"),
+                        control=c0.detach().numpy(), J=np.array(float(J)),
+                        dJ_dc=c0.grad.numpy(), dJ_dfields=np.stack([f.grad.numpy() for f in fields]),
+                        vals=sol.vals.detach().numpy())
+    print("adjoint: J =", float(J))
+
+
+if __name__ == "__main__":
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    updes = load_reference(ref)
+    only = sys.argv[2:] or list(C.CASES)
+    for name in only:
+        if name == "adjoint":
+            continue
+        run_case(updes, name, C.CASES[name])
+    if len(sys.argv) <= 2 or "adjoint" in sys.argv[2:]:
+        run_adjoint(updes)
