@@ -1,0 +1,347 @@
+"""Benchmark: solves/s of the global RBF collocation solve at N = 22,500 nodes.
+
+Workload (the Poisson manufactured-solution configuration): SquareCloud
+Nx = Ny = 150 (N = 22,500), interior nodes jittered by U(-0.2h, 0.2h) from a
+seed, all facets Dirichlet u* = sin(pi x) sin(pi y), rhs -2 pi^2 u*,
+polyharmonic r^3, max_degree = 2 (n = N + 6 = 22,506).  Synthetic, generated
+here; no dataset exists for it.
+
+A step is one complete solve of a fresh system: assemble the Kansa matrix,
+equilibrate, factor, refine to the stopping test, evaluate vals.  `value` is
+the FP32-LU + FP64-GMRES path with inputs resident in HBM; `fp64_lu` is the
+plain FP64 LU path on the same GPU; `e2e` is the same metric through the
+public API (`updes_gb300.pde_solver`: host capture of the operator, host
+arrays copied in, vals and coeffs copied out).  The matrices (4-10 GB) are far
+larger than L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s at N=22.5k: FP32-LU+FP64 IR vs FP64 LU, same GB300, rel err<=1e-8"
+UNIT = "solves/s"
+
+
+def workload_spec(nx):
+    return {"workload": f"poisson_manufactured_r3_deg2_jitter0.2_N{nx * nx}", "nodes": nx * nx,
+            "n": nx * nx + 6, "rbf": "polyharmonic r^3", "max_degree": 2, "jitter": "U(-0.2h,0.2h) seed 0",
+            "facets": "all Dirichlet", "l2": "inputs larger than L2 (matrices >= 4 GB)"}
+
+
+def make_problem(nx, U):
+    facets = {"South": "d", "West": "d", "North": "d", "East": "d"}
+    cloud = U.SquareCloud(Nx=nx, Ny=nx, facet_types=facets, jitter=(0.2, 0))
+    ustar = lambda c: np.sin(np.pi * c[0]) * np.sin(np.pi * c[1])
+    op = lambda x, center, rbf, monomial, fields: U.nodal_laplacian(x, center, rbf, monomial)
+    rhs = lambda x, centers, rbf, fields: -2 * np.pi ** 2 * np.sin(np.pi * x[0]) * np.sin(np.pi * x[1])
+    bcs = {f: ustar for f in facets}
+    return cloud, op, rhs, bcs, ustar
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(nx_sample, n_full):
+    """The oracle's restatement of the reference's solve (inv -> GEMM -> QR -> inv) at a bounded
+    sample size, on all host cores; scaled to the full size by (n_full / n_sample)^3."""
+    from oracle import updes_np as O
+    facets = {"South": "d", "West": "d", "North": "d", "East": "d"}
+    xs = np.linspace(0, 1, nx_sample)
+    h = xs[1] - xs[0]
+    coords = np.stack(np.meshgrid(xs, xs, indexing="ij"), -1).reshape(-1, 2)
+    ii, jj = np.divmod(np.arange(nx_sample * nx_sample), nx_sample)
+    inner = (ii > 0) & (ii < nx_sample - 1) & (jj > 0) & (jj < nx_sample - 1)
+    coords[inner] += np.random.default_rng(0).uniform(-0.2 * h, 0.2 * h, size=(inner.sum(), 2))
+    t0 = time.perf_counter()
+    cl = O.square_cloud(nx_sample, nx_sample, facets, coords=coords)
+    X = cl.sorted_nodes
+    W = np.zeros((cl.Ni, 5)); W[:, 3:] = 1.0
+    K = O.assemble_K(cl, "polyharmonic", 1, 2, W, O.boundary_rows(cl, {}))
+    A = O.assemble_A(cl, "polyharmonic", 1, 2)
+    us = np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1])
+    q = np.where(np.arange(cl.N) < cl.Ni, -2 * np.pi ** 2 * us, us)
+    t1 = time.perf_counter()
+    O.solve_faithful(K, A, q)
+    t2 = time.perf_counter()
+    n_s = cl.N + 6
+    r = n_full / n_s
+    # assembly is O(n^2), the inverse / GEMM / QR O(n^3)
+    return t2 - t0, (t1 - t0) * r ** 2 + (t2 - t1) * r ** 3, n_s
+
+
+def cpu_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        return max(int(i.get("num_threads", 1)) for i in threadpool_info()) or os.cpu_count()
+    except Exception:
+        return os.cpu_count()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU path (the oracle port: the reference needs JAX, which is not installed)."""
+    if rank != 0:
+        return
+    n_full = args.nx * args.nx + 6
+    for _ in range(args.warmup):
+        cpu_sample(args.sample_nx, n_full)
+    times = []
+    for _ in range(args.steps):
+        dt, scaled, n_s = cpu_sample(args.sample_nx, n_full)
+        times.append(scaled)
+    ms = 1000.0 * statistics.mean(times)
+    value = 1000.0 / ms
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_spec(args.nx),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+                             "sample": f"oracle restatement of the reference solve (inv->GEMM->QR->inv, FP64 "
+                                       f"LAPACK) at N={args.sample_nx ** 2} (n={args.sample_nx ** 2 + 6}) per step; assembly "
+                                       f"scaled by (n/n_sample)^2 and the solve by (n/n_sample)^3 to n={n_full}; "
+                                       f"JAX is not installed, so the "
+                                       f"reference itself cannot run"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import updes_gb300 as U
+    from updes_gb300 import _lib
+    from updes_gb300.operators import DeviceProblem, SolverOptions, prepare, solve_device
+
+    torch.cuda.set_device(local)
+    cloud, op, rhs, bcs, ustar = make_problem(args.nx, U)
+    opts32 = SolverOptions(precision="fp32")
+    opts64 = SolverOptions(precision="fp64")
+    W, kind, bnodes, geom, q = prepare(op, rhs, cloud, bcs, U.polyharmonic, 2, options=opts32)
+    dp = DeviceProblem(cloud, U.polyharmonic, 2, W, kind, bnodes, geom)
+    qd = torch.as_tensor(q, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, steps, warmup, with_stats=False, clocks=None):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        _lib.stats_reset(timing=with_stats)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ctx = clocks if clocks is not None else _Null()
+        with ctx:
+            ev0.record(stream)
+            for _ in range(steps):
+                fn()
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        barrier(world)
+        ms = ev0.elapsed_time(ev1)
+        return max_over_ranks(ms, world), _lib.stats_read()
+
+    # accuracy references
+    c64, v64, info64 = solve_device(dp, qd, opts64)
+    c32, v32, info32 = solve_device(dp, qd, opts32)
+    X = cloud.sorted_nodes
+    us = ustar(X.T)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    v32h, v64h = v32.cpu().numpy(), v64.cpu().numpy()
+
+    sampler = ClockSampler(local)
+    ms32, st32 = timed(lambda: solve_device(dp, qd, opts32), args.steps, args.warmup, with_stats=True, clocks=sampler)
+    clocks = sampler.summary()
+    ms64, st64 = timed(lambda: solve_device(dp, qd, opts64), args.fp64_steps, 1)
+
+    # end to end through the public API (host arrays in, vals/coeffs out)
+    def e2e_call():
+        sol = U.pde_solver(op, rhs, cloud, bcs, U.polyharmonic, 2, options=opts32)
+        return sol
+    ms_e2e, _ = timed(e2e_call, max(1, args.e2e_steps), 1)
+    h2d = (cloud.N * 2 * 8 + cloud.Ni * 5 * 8 + (cloud.N - cloud.Ni) * (4 * 2 + 4 + 8 * 8) + cloud.N * 8)
+    d2h = cloud.N * 8 + (cloud.N + 6) * 8
+
+    steps = args.steps
+    value = world * steps / (ms32 / 1000.0)
+    per = {k: v for k, v in st32["by_class"].items() if v["count"]}
+    dom = max(per, key=lambda k: per[k]["ms"])
+    d = per[dom]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    tensor_kernel = bool(_lib.load() and U.operators.__dict__.get("TENSOR_UPDATE", False))
+    if dom == "trailing_update" and tensor_kernel:
+        achieved = d["flops"] / (d["ms"] / 1000.0) / 1e12
+        peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "measured bf16 sustained" if "bf16_tflops_sustained" in peaks else "fallback"}
+    elif dom == "trailing_update":
+        achieved = d["flops"] / (d["ms"] / 1000.0) / 1e12
+        roof = {"bound": "fp64-alu", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s", "frac": achieved / 1.25,
+                "peak_source": "nominal FP64 (no measured FP64 peak available)"}
+    else:
+        achieved = d["bytes"] / (d["ms"] / 1000.0) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    roof.update({"kernel": dom, "launches": d["count"] // steps, "avg_launch_ms": d["ms"] / d["count"],
+                 "algorithmic_per_launch": (d["flops"] if roof["unit"] == "TFLOP/s" else d["bytes"]) / d["count"]})
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(dom)
+    except Exception:
+        pass
+    roof["traffic"] = traffic
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        dt, scaled, n_s = cpu_sample(args.sample_nx, args.nx * args.nx + 6)
+        cpu = {"value": 1000.0 / (scaled * 1000.0), "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+               "sample": f"oracle restatement of the reference solve (inv->GEMM->QR->inv) at N={args.sample_nx ** 2}: "
+                         f"{dt:.2f} s; assembly scaled by (n/n_sample)^2, solve by (n/n_sample)^3 "
+                         f"(n/n_sample = {(args.nx ** 2 + 6) / n_s:.2f})"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms32 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32-lu+f64", "data": "synthetic",
+        "config": {**workload_spec(args.nx), "parallelism": "replicas" if world > 1 else "single"},
+        "fp64_lu": {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": UNIT,
+                    "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
+        "speedup_vs_fp64_lu": (ms64 / args.fp64_steps) / (ms32 / steps),
+        "accuracy": {"rel_err_vals_vs_fp64_lu": rel(v32h, v64h), "rel_err_vals_vs_exact": rel(v32h, us),
+                     "fp64_rel_err_vs_exact": rel(v64h, us), "gmres_iters": info32["iters"],
+                     "fell_back": info32["fell_back"], "backward_error": info32["backward_error"],
+                     "fp64_backward_error": info64["backward_error"]},
+        "phases_ms": {k: info32[k] for k in ("t_assemble_ms", "t_factor_ms", "t_refine_ms", "t_eval_ms")},
+        "e2e": {"value": world * max(1, args.e2e_steps) / (ms_e2e / 1000.0), "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": roof, "clocks": clocks, "gpu_launches": st32["launches"],
+        "kernel_ms_per_step": {k: v["ms"] / steps for k, v in per.items()},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nx", type=int, default=150)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--sample-nx", type=int, default=70)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

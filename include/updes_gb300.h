@@ -1,0 +1,230 @@
+/*
+ * updes_gb300.h — C ABI of the GB300 global RBF collocation solver.
+ *
+ * This is the drop-in boundary for the hot path of Updes' `pde_solver` /
+ * `pde_solver_jit` with support_size="max" (updes/operators.py:559-683).
+ * Every pointer named "device" is a CUDA device pointer owned by the caller;
+ * matrices are row-major with an explicit leading dimension.  `stream` is a
+ * cudaStream_t passed as void* so that this header needs no CUDA include.
+ * No entry point aborts, traps or allocates device memory: device-side
+ * failures are reported through an integer status (and, where stated, an
+ * `info` word), and scratch memory is a caller-provided workspace whose size
+ * the matching *_workspace query returns.
+ *
+ * Python callers bind these symbols with ctypes (updes_gb300/_lib.py); the
+ * reference-side binding a maintainer would add is shown in INTEGRATION.md.
+ */
+#ifndef UPDES_GB300_H
+#define UPDES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define UPDES_API __attribute__((visibility("default")))
+#else
+#define UPDES_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  UPDES_OK = 0,
+  UPDES_ERR_INVALID = 1,        /* bad argument (size, pointer, enum)            */
+  UPDES_ERR_CUDA = 2,           /* a CUDA runtime call failed                    */
+  UPDES_ERR_SINGULAR = 3,       /* LU met an exactly zero or non-finite pivot    */
+  UPDES_ERR_NOT_CONVERGED = 4,  /* refinement stalled or hit its iteration cap   */
+  UPDES_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up            */
+  UPDES_ERR_UNSUPPORTED = 6,    /* valid request this build does not implement   */
+  UPDES_ERR_WORKSPACE = 7       /* workspace too small                           */
+};
+
+/* ---- radial basis functions (updes/utils.py:30-69) --------------------- */
+enum {
+  UPDES_RBF_POLYHARMONIC = 0,          /* r^(2a+1),            param = a   */
+  UPDES_RBF_GAUSSIAN = 1,              /* exp(-(eps r)^2),     param = eps */
+  UPDES_RBF_MULTIQUADRIC = 2,          /* sqrt(1+(eps r)^2),   param = eps */
+  UPDES_RBF_INVERSE_MULTIQUADRIC = 3,  /* 1/sqrt(1+(eps r)^2), param = eps */
+  UPDES_RBF_THIN_PLATE = 4             /* log(r) r^(2a),       param = a   */
+};
+
+/* ---- boundary row kinds (updes/assembly.py:141-362) -------------------- */
+enum {
+  UPDES_ROW_DIRICHLET = 0,       /* phi(x_i, x_j)                                  */
+  UPDES_ROW_NEUMANN = 1,         /* grad phi(x_i, x_j) . n1                        */
+  UPDES_ROW_ROBIN = 2,           /* beta phi + grad phi . n1                       */
+  UPDES_ROW_PERIODIC_VALUE = 3,  /* phi(x_i, x_j) - phi(x_p, x_j), every column    */
+  UPDES_ROW_PERIODIC_FLUX = 4    /* grad phi(x_i).n1 + grad phi(x_p).n2, every col */
+};
+
+/* ---- precisions of the factorisation ----------------------------------- */
+enum {
+  UPDES_PREC_FP64 = 0,   /* FP64 LU (the plain path)                               */
+  UPDES_PREC_FP32 = 1    /* FP32 LU + FP64 GMRES iterative refinement               */
+};
+
+/*
+ * One collocation problem on one cloud.  Row order is the reference's sorted
+ * node order (internal, Dirichlet, Neumann, Robin, periodic;
+ * updes/cloud.py:124-150), so row r < Ni is an interior operator row and row
+ * Ni <= r < N is boundary row r - Ni.  n = N + M.
+ */
+typedef struct {
+  int32_t N;                  /* nodes                                              */
+  int32_t Ni;                 /* interior nodes (rows carrying the PDE operator)     */
+  int32_t M;                  /* monomials: 1, 3, 6, 10 or 15 (max_degree 0..4)       */
+  int32_t rbf;                /* UPDES_RBF_*                                          */
+  double rbf_param;           /* a (polyharmonic, thin plate) or eps                  */
+  int32_t self_term;          /* 0 = the reference's zero diagonal in Phi blocks      */
+  int32_t reserved;
+  const double* nodes;        /* device, N x 2, (x, y) per node                       */
+  const double* op_weights;   /* device, Ni x 5: value, d/dx, d/dy, d2/dx2, d2/dy2    */
+  const int32_t* bd_kind;     /* device, N - Ni: UPDES_ROW_*                          */
+  const int32_t* bd_node;     /* device, (N - Ni) x 2: evaluation node, partner node  */
+  const double* bd_geom;      /* device, (N - Ni) x 8: n1x n1y n2x n2y nPx nPy beta 0 */
+} updes_problem;
+
+/* Library version (major*10000 + minor*100 + patch). */
+UPDES_API int updes_version(void);
+
+/* Human-readable text of a status code. */
+UPDES_API const char* updes_status_string(int status);
+
+/* Text of the last CUDA runtime failure seen by the library (thread-safe copy). */
+UPDES_API const char* updes_last_error(void);
+
+/* Padded leading dimension used for an n x n matrix of `elem_bytes` elements
+ * (a multiple of 32 elements, so rows start on 128-byte boundaries). */
+UPDES_API int64_t updes_matrix_ld(int64_t n, int32_t elem_bytes);
+
+/*
+ * Assemble the augmented Kansa matrix
+ *     K = [[op(Phi), op(P)], [bd(Phi), bd(P)], [P^T, 0]]     (n x n)
+ * in FP64 (K64) and/or FP32 (K32, the rounding of the FP64 entries); either
+ * output may be NULL.  Entries are computed in FP64 with closed-form kernel
+ * derivatives.  Columns n..ld-1 are written as zero.
+ * Replaces assemble_op_Phi_P (updes/assembly.py:93-137), assemble_bd_Phi_P
+ * (assembly.py:141-362) and the P^T block of assemble_A (assembly.py:62-85);
+ * the reference multiplies [op; bd] by inv(A) instead (assembly.py:366-401).
+ */
+UPDES_API int updes_assemble(const updes_problem* p, double* K64, int64_t ld64, float* K32, int64_t ld32,
+                   void* stream);
+
+/*
+ * vals = [Phi P] c at the nodes (Phi_ii = 0 unless self_term), FP64,
+ * regenerating Phi on the fly.  coeffs: device, n; vals: device, N.
+ * Replaces the `vals` of the reference, which come out of its QR solve
+ * (updes/operators.py:612-613) and satisfy A c = [vals; 0] (assembly.py:404-410).
+ */
+UPDES_API int updes_eval_values(const updes_problem* p, const double* coeffs, double* vals, void* stream);
+
+/*
+ * Field value (what = 0, out: m), gradient (what = 1, out: m x 2) or Laplacian
+ * (what = 2, out: m) at m arbitrary points from coefficients c (N + M) on the
+ * N centers, summing over every center (phi(0) included, derivatives 0 there).
+ * Replaces value / gradient / laplacian (updes/operators.py:118-184, 319-348).
+ */
+UPDES_API int updes_eval_field(int32_t m, const double* points, int32_t N, const double* centers, int32_t M,
+                               int32_t rbf, double rbf_param, const double* coeffs, int32_t what, double* out,
+                               void* stream);
+
+/*
+ * Workspace bytes for updes_lu_factor / updes_lu_solve on an n x n matrix.
+ */
+UPDES_API int updes_lu_workspace(int32_t n, int32_t precision, size_t* bytes);
+
+/*
+ * LU with partial pivoting, P A = L U (L unit lower), row-major.
+ * A: device FP64 n x lda, the matrix; it is used as the working storage and
+ * destroyed.  Factors go to F (device, n x ldf): with UPDES_PREC_FP64, F is
+ * FP64 and may be A itself (in-place); with UPDES_PREC_FP32, F is FP32 and
+ * receives L and U rounded to FP32 while every Schur-complement update is
+ * accumulated in FP64 in A (FP32 factors of an FP64-accurate elimination).
+ * piv: device, 2n ints: [0, n) the interchanges (row k swapped with piv[k] at
+ * step k, LAPACK getrf convention, 0-based), [n, 2n) the resulting row
+ * permutation (row i of P A is row piv[n + i] of A).
+ * info: host; 0, or 1 + the first step whose pivot was exactly zero or
+ * non-finite (the factorisation still runs to the end, like LAPACK).
+ * Replaces the LAPACK getrf behind jnp.linalg.inv (updes/assembly.py:87-90)
+ * and the lineax QR factorisation (updes/operators.py:612-613).
+ */
+UPDES_API int updes_lu_factor(int32_t n, double* A, int64_t lda, int32_t precision, void* F, int64_t ldf, int32_t* piv,
+                    void* workspace, size_t workspace_bytes, int32_t* info, void* stream);
+
+/*
+ * Solve with the factors of updes_lu_factor: x = A^-1 b (trans = 0) or
+ * x = A^-T b (trans = 1) for `nrhs` right-hand sides stored as the columns of
+ * the row-major n x nrhs block b (leading dimension ldb), overwritten by x.
+ * Arithmetic is FP64 for both factor precisions.  The transpose solve is the
+ * adjoint's (the reference differentiates through lineax instead).
+ */
+UPDES_API int updes_lu_solve(int32_t n, const void* F, int64_t ldf, int32_t precision, const int32_t* piv, double* b,
+                   int32_t nrhs, int64_t ldb, int32_t trans, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
+/* r = b - K x (trans = 0) or r = b - K^T x (trans = 1) with FP64 K, x, b, r (device, n). */
+UPDES_API int updes_residual(int32_t n, const double* K, int64_t ldk, const double* x, const double* b,
+                   double* r, int32_t trans, void* stream);
+
+/* ---- the full solve ------------------------------------------------------ */
+
+typedef struct {
+  int32_t precision;      /* UPDES_PREC_FP64 or UPDES_PREC_FP32                          */
+  int32_t max_iters;      /* refinement cap (GMRES iterations in total)                  */
+  int32_t restart;        /* GMRES restart length                                        */
+  int32_t fallback_fp64;  /* 1: if refinement stalls, refactor in FP64 and solve again    */
+  double tol;             /* stop when ||b - K c|| <= tol ||b||, or when the componentwise
+                             backward error reaches the FP64 floor (64 unit roundoffs)      */
+} updes_solve_opts;
+
+typedef struct {
+  int32_t iters;          /* GMRES iterations of the FP32-LU attempt (0 for the FP64 path)      */
+  int32_t fell_back;      /* 1 if the FP64 fallback ran                                        */
+  int32_t lu_info;        /* info of the last factorisation                                    */
+  int32_t converged;      /* 1 if the stopping test was met                                    */
+  double rel_residual;    /* final ||b - K c|| / ||b|| (equilibrated system)                   */
+  double backward_error;  /* final max_i |b - K c|_i / (|K| |c| + |b|)_i (equilibrated system) */
+  double t_assemble_ms, t_factor_ms, t_refine_ms, t_eval_ms;
+} updes_solve_info;
+
+/* Workspace bytes for updes_solve (matrices, factors and Krylov basis). */
+UPDES_API int updes_solve_workspace(const updes_problem* p, const updes_solve_opts* opts, size_t* bytes);
+
+/*
+ * Assemble, factor and solve K c = [q; 0], then vals = [Phi P] c.
+ * q: device, N (interior rhs then boundary values in sorted order);
+ * coeffs: device, n; vals: device, N (may be NULL).
+ * Replaces pde_solver's assemble_B → lineax QR → core_compute_coefficients
+ * sequence (updes/operators.py:602-618).
+ */
+UPDES_API int updes_solve(const updes_problem* p, const double* q, double* coeffs, double* vals,
+                const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                size_t workspace_bytes, void* stream);
+
+/* ---- instrumentation ------------------------------------------------------ */
+
+/* Kernel classes of updes_stats: 0 trailing update, 1 panel, 2 TRSM, 3 triangular
+ * solves, 4 FP64 GEMV/residual, 5 assembly, 6 other. */
+#define UPDES_STAT_CATEGORIES 7
+
+typedef struct {
+  int64_t launches;                       /* kernels launched since the last reset        */
+  int64_t count[UPDES_STAT_CATEGORIES];   /* timed launches per class                      */
+  double ms[UPDES_STAT_CATEGORIES];       /* summed CUDA-event time per class              */
+  double flops[UPDES_STAT_CATEGORIES];    /* algorithmic flops of the timed launches       */
+  double bytes[UPDES_STAT_CATEGORIES];    /* algorithmic bytes of the timed launches       */
+} updes_stats;
+
+/* Zero the counters; enable_timing = 1 brackets every launch with CUDA events on
+ * its stream (adds a little host overhead).  Not part of the reference. */
+UPDES_API void updes_stats_reset(int32_t enable_timing);
+UPDES_API void updes_stats_read(updes_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UPDES_GB300_H */

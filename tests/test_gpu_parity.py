@@ -1,0 +1,199 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the reference's golden vectors."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import cases as C
+from golden_problem import case_of, load, oracle_problem
+from gpu_helpers import assemble, device_problem, solve_case
+from oracle import updes_np as O
+from updes_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+NAMES = list(C.CASES)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("compat", [True, False])
+def test_assembly_matches_oracle(name, compat):
+    """Every assembled entry within 1e-12 of the oracle, relative to its row's scale."""
+    case = case_of(load(name))
+    p = oracle_problem(case, compat=compat)
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
+    cl, dp, q = device_problem(case, compat=compat)
+    K64, K32, ld = assemble(dp, fp32=True)
+    Kg = K64.cpu().numpy()
+    n = dp.n
+    assert np.all(Kg[:, n:] == 0.0)
+    Kg = Kg[:, :n]
+    scale = np.abs(K).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(Kg - K) / scale) < 1e-12
+    assert np.array_equal(K32.cpu().numpy()[:, :n], Kg.astype(np.float32))
+    assert np.allclose(q, p["q"], rtol=1e-12, atol=1e-12 * np.abs(p["q"]).max())
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_assembly_against_reference_rows(name):
+    """The same entries against the reference's own matrices (golden)."""
+    g = load(name)
+    case = case_of(g)
+    cl, dp, q = device_problem(case)
+    K64, _, _ = assemble(dp)
+    Kg = K64.cpu().numpy()[:cl.N, :dp.n]
+    if "diffMat" in g:
+        ref, rows = g["diffMat"], np.arange(cl.N)
+    else:
+        ref, rows = g["diffMat_sub"], g["diffMat_rows"]
+    scale = np.abs(ref).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(Kg[rows] - ref) / scale) < 1e-12
+    assert rel(q, g["q"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_eval_kernels(name):
+    import torch
+    g = load(name)
+    case = case_of(g)
+    cl, dp, q = device_problem(case)
+    lib = _lib.load()
+    c = torch.as_tensor(g["coeffs"], device="cuda")
+    vals = torch.empty(cl.N, dtype=torch.float64, device="cuda")
+    _lib.check(lib.updes_eval_values(ctypes.byref(dp.c), c.data_ptr(), vals.data_ptr(), dp.stream()), "eval")
+    p = oracle_problem(case)
+    want = O.eval_values(p["cloud"], p["kind"], p["param"], p["deg"], g["coeffs"])
+    assert rel(vals.cpu().numpy(), want) < 1e-12
+    import updes_gb300 as U
+    from gpu_helpers import rbf_callable
+    X = cl.sorted_nodes
+    assert rel(U.value_vec(X, g["coeffs"], X, rbf_callable(case)), g["value_at_nodes"]) < 1e-12
+    assert rel(U.gradient_vec(X, g["coeffs"], X, rbf_callable(case)), g["grad_at_nodes"]) < 1e-12
+    lap = U.laplacian_vec(X, g["coeffs"], X, rbf_callable(case))
+    t = O.rbf_terms(p["kind"], p["param"], X[:, 0:1] - X[None, :, 0], X[:, 1:2] - X[None, :, 1])
+    want_lap = (t[3] + t[4]) @ g["coeffs"][:cl.N] + sum(
+        g["coeffs"][cl.N + k] * (lambda m: m[3] + m[4])(O.monomial_terms(k, X[:, 0], X[:, 1]))
+        for k in range(dp.M))
+    assert rel(lap, want_lap) < 1e-12
+
+
+def _floor(g, p):
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
+    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"])
+    u, c = O.solve_direct(K, A, p["q"])
+    return rel(u, g["vals"]), u
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_solve_matches_reference(name, precision):
+    """vals within 1e-10 (FP64 path) / 1e-8 (FP32 LU + FP64 GMRES) of the reference, or within 3x the
+    oracle's own distance to the reference where that floor is larger."""
+    import updes_gb300 as U
+    g = load(name)
+    case = case_of(g)
+    p = oracle_problem(case)
+    floor, u_or = _floor(g, p)
+    cl, sol = solve_case(case, precision)
+    tol = (1e-10 if precision == "fp64" else 1e-8)
+    err = rel(sol.vals, g["vals"])
+    assert err <= max(tol, 3 * floor), (err, floor, U.LAST_INFO)
+    assert rel(sol.vals, u_or) <= max(tol, 3 * floor)
+    assert U.LAST_INFO["converged"] == 1
+    if precision == "fp32":
+        assert U.LAST_INFO["fell_back"] == 0, U.LAST_INFO
+
+
+def test_mat_materialises_reference_B():
+    g = load("poisson_jitter_11x11")
+    case = case_of(g)
+    cl, sol = solve_case(case, "fp64")
+    B = sol.mat.materialize()
+    assert B.shape == (cl.N, cl.N)
+    assert rel(B, g["B"]) < 1e-9
+
+
+def _rand_system(n, seed):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((n, n)) + 0.5 * np.eye(n)
+    return A
+
+
+@pytest.mark.parametrize("n", [1, 7, 64, 65, 200, 513])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_lu_solve_random(n, precision):
+    import torch
+    lib = _lib.load()
+    A = _rand_system(n, n)
+    ld = int(lib.updes_matrix_ld(n, 8))
+    Ad = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+    Ad[:, :n] = torch.as_tensor(A)
+    F = torch.zeros((n, ld), dtype=torch.float32, device="cuda") if precision else None
+    piv = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    nb = ctypes.c_size_t()
+    _lib.check(lib.updes_lu_workspace(n, precision, ctypes.byref(nb)), "ws")
+    ws = torch.empty(nb.value + 8 * n * 4 + 1024, dtype=torch.uint8, device="cuda")
+    info = ctypes.c_int32(-1)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.updes_lu_factor(n, Ad.data_ptr(), ld, precision, F.data_ptr() if precision else None,
+                                   ld if precision else 0, piv.data_ptr(), ws.data_ptr(), ws.numel(),
+                                   ctypes.byref(info), s), "factor")
+    assert info.value == 0
+    Fp = F if precision else Ad
+    # pivots follow LAPACK's choice (max |a|, first on ties) in the FP64 path
+    if precision == 0:
+        import scipy.linalg as sla
+        lu, pv = sla.lu_factor(A)
+        assert np.array_equal(piv[:n].cpu().numpy(), pv)
+        assert np.allclose(Ad[:, :n].cpu().numpy(), lu, rtol=1e-10, atol=1e-10)
+    rng = np.random.default_rng(1)
+    B = rng.standard_normal((n, 3))
+    for trans in (0, 1):
+        Bd = torch.as_tensor(B.copy(), device="cuda")
+        _lib.check(lib.updes_lu_solve(n, Fp.data_ptr(), ld, precision, piv.data_ptr(), Bd.data_ptr(), 3, 3, trans,
+                                      ws.data_ptr(), ws.numel(), s), "solve")
+        X = Bd.cpu().numpy()
+        want = np.linalg.solve(A.T if trans else A, B)
+        tol = 1e-10 if precision == 0 else 1e-3
+        assert rel(X, want) < tol, (trans, rel(X, want))
+
+
+def test_lu_reports_singular_pivot():
+    import torch
+    lib = _lib.load()
+    n = 96
+    A = _rand_system(n, 5)
+    A[:, 17] = 0.0
+    ld = int(lib.updes_matrix_ld(n, 8))
+    Ad = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+    Ad[:, :n] = torch.as_tensor(A)
+    piv = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    nb = ctypes.c_size_t()
+    lib.updes_lu_workspace(n, 0, ctypes.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    info = ctypes.c_int32(0)
+    st = lib.updes_lu_factor(n, Ad.data_ptr(), ld, 0, None, 0, piv.data_ptr(), ws.data_ptr(), ws.numel(),
+                             ctypes.byref(info), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0 and info.value == 18
+
+
+def test_residual_kernel():
+    import torch
+    lib = _lib.load()
+    n = 300
+    A = _rand_system(n, 9)
+    ld = int(lib.updes_matrix_ld(n, 8))
+    Ad = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+    Ad[:, :n] = torch.as_tensor(A)
+    rng = np.random.default_rng(2)
+    x, b = rng.standard_normal(n), rng.standard_normal(n)
+    xd, bd = torch.as_tensor(x, device="cuda"), torch.as_tensor(b, device="cuda")
+    r = torch.empty(n, dtype=torch.float64, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for trans in (0, 1):
+        _lib.check(lib.updes_residual(n, Ad.data_ptr(), ld, xd.data_ptr(), bd.data_ptr(), r.data_ptr(), trans, s), "r")
+        want = b - (A.T if trans else A) @ x
+        assert rel(r.cpu().numpy(), want) < 1e-13

@@ -1,0 +1,175 @@
+"""Host-side logic (no GPU): cloud ordering, row descriptors, operator capture, C-ABI exports."""
+import ctypes
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cases as C
+import updes_gb300 as U
+from golden_problem import case_of, load, oracle_problem
+from oracle import updes_np as O
+from updes_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+NAMES = list(C.CASES)
+
+
+def product_cloud(case):
+    return U.SquareCloud(Nx=case["Nx"], Ny=case["Ny"], facet_types=dict(case["facets"]),
+                         coords=C.grid_coords(case))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_cloud_matches_reference(name):
+    g = load(name)
+    case = case_of(g)
+    cl = product_cloud(case)
+    assert np.array_equal(cl.sorted_nodes, g["sorted_nodes"])
+    assert [cl.N, cl.Ni, cl.Nd, cl.Nn, cl.Nr, sum(cl.Np)] == g["counts"].tolist()
+    assert cl.facet_nodes == json.loads(str(g["facet_nodes"]))
+    assert np.array_equal(cl.sorted_outward_normals.reshape(-1, 2), g["sorted_outward_normals"].reshape(-1, 2))
+
+
+def test_jitter_matches_case_generator():
+    case = C.CASES["poisson_jitter_11x11"]
+    a = U.SquareCloud(Nx=11, Ny=11, facet_types=dict(case["facets"]), jitter=case["jitter"])
+    b = product_cloud(case)
+    assert np.array_equal(a.sorted_nodes, b.sorted_nodes)
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("compat", [True, False])
+def test_boundary_rows_match_oracle(name, compat):
+    g = load(name)
+    case = case_of(g)
+    p = oracle_problem(case, compat=compat)
+    cl = product_cloud(case)
+    rows = p["rows"]
+    _, robin = U.operators._bc_values_and_betas(_bcs(case, cl), cl, compat)
+    kind, nodes, geom = U.operators.boundary_rows(cl, robin, compat)
+    assert np.array_equal(kind, rows.kind)
+    assert np.array_equal(nodes[:, 0], rows.i1) and np.array_equal(nodes[:, 1], rows.i2)
+    assert np.array_equal(geom[:, 0:2], rows.n1)
+    per = rows.kind >= O.ROW_PD
+    assert np.array_equal(geom[per, 2:4], rows.n2[per])
+    assert np.array_equal(geom[:, 4:6], rows.nP)
+    assert np.array_equal(geom[:, 6], rows.beta)
+
+
+def _bcs(case, cl):
+    out = {}
+    for f, spec in case["bc"].items():
+        fn = lambda name: (lambda x: C.FUNCS[name](np, x[0], x[1]))
+        out[f] = (fn(spec[0]), fn(spec[1])) if isinstance(spec, tuple) else fn(spec)
+    return out
+
+
+def _diff_operator(op):
+    """The golden cases' operators written against updes_gb300's nodal operators."""
+    def f(x, center=None, rbf=None, monomial=None, fields=None):
+        val = U.nodal_value(x, center, rbf, monomial)
+        grad = U.nodal_gradient(x, center, rbf, monomial)
+        lap = U.nodal_laplacian(x, center, rbf, monomial)
+        if op == "laplacian":
+            return lap
+        if op == "advdiff":
+            return val / C.ADV_DT + np.dot(np.array(C.ADV_VEL), grad) - C.ADV_K * lap
+        if op == "kgrad":
+            return fields[0] * lap + fields[1] * grad[0] + fields[2] * grad[1]
+        if op == "darcy":
+            return U.nodal_div_grad(x, center, rbf, monomial, (fields[0], fields[0])) + fields[1] * val
+        if op == "helmholtz_x":
+            return lap + (1.0 + x[0] * x[1]) * val
+        raise ValueError(op)
+    return f
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_operator_capture(name):
+    g = load(name)
+    case = case_of(g)
+    cl = product_cloud(case)
+    X = cl.sorted_nodes[:cl.Ni]
+    fields = C.make_fields(case, cl.sorted_nodes)
+    W = U.capture_operator(_diff_operator(case["op"]), X, U.polyharmonic,
+                           None if fields is None else fields[:, :cl.Ni])
+    ref = C.op_weights(case["op"], X[:, 0], X[:, 1], None if fields is None else fields[:, :cl.Ni])
+    assert np.allclose(W, ref, rtol=1e-14, atol=1e-14)
+
+
+def test_capture_rejects_nonlinear():
+    X = np.random.default_rng(0).uniform(size=(5, 2))
+    with pytest.raises(ValueError):
+        U.capture_operator(lambda x, c, r, m, f: U.nodal_value(x, c, r, m) ** 2, X, U.polyharmonic, None)
+    with pytest.raises(ValueError):
+        U.capture_operator(lambda x, c, r, m, f: U.nodal_laplacian(x, c, r, m) + 1.0, X, U.polyharmonic, None)
+
+
+def test_capture_per_node_fallback():
+    """An operator that only works on one point at a time is captured node by node."""
+    X = np.random.default_rng(0).uniform(size=(7, 2))
+
+    def op(x, center, rbf, monomial, fields):
+        assert np.asarray(x).shape == (2,)
+        vel = np.array([x[1], -x[0]])
+        return vel @ U.nodal_gradient(x, center, rbf, monomial) + U.nodal_laplacian(x, center, rbf, monomial)
+    W = U.capture_operator(op, X, U.polyharmonic, None)
+    assert np.allclose(W[:, 1], X[:, 1]) and np.allclose(W[:, 2], -X[:, 0]) and np.allclose(W[:, 3:], 1.0)
+
+
+def test_rbf_spec():
+    from functools import partial
+    assert U.rbf_spec(U.polyharmonic) == (_lib.RBF_POLYHARMONIC, 1.0)
+    assert U.rbf_spec(partial(U.polyharmonic, a=2)) == (_lib.RBF_POLYHARMONIC, 2.0)
+    assert U.rbf_spec(partial(U.gaussian, eps=3.0)) == (_lib.RBF_GAUSSIAN, 3.0)
+    with pytest.raises(ValueError):
+        U.rbf_spec(lambda x, c: 1.0)
+    with pytest.raises(ValueError):
+        U.rbf_spec(partial(U.polyharmonic, a=1.5))
+
+
+def test_nodal_numeric_matches_oracle():
+    rng = np.random.default_rng(3)
+    for kind, p in [("polyharmonic", 2), ("gaussian", 2.0), ("multiquadric", 1.5), ("inverse_multiquadric", 0.7),
+                    ("thin_plate", 1)]:
+        rbf = getattr(U, kind)
+        from functools import partial
+        rbf = partial(rbf, **({"a": p} if kind in ("polyharmonic", "thin_plate") else {"eps": p}))
+        x, c = rng.uniform(size=2), rng.uniform(size=2)
+        t = O.rbf_terms(kind, p, x[0] - c[0], x[1] - c[1])
+        assert np.isclose(U.nodal_value(x, c, rbf), t[0], rtol=1e-13)
+        assert np.allclose(U.nodal_gradient(x, c, rbf), [t[1], t[2]], rtol=1e-13)
+        assert np.isclose(U.nodal_laplacian(x, c, rbf), t[3] + t[4], rtol=1e-13)
+        assert np.isclose(rbf(x, c), t[0], rtol=1e-13)
+
+
+def test_library_exports_every_declared_symbol():
+    """The C-ABI library loads and exports every function include/updes_gb300.h declares."""
+    if not os.path.exists(_lib.LIB_PATH):
+        from updes_gb300 import build
+        build.build()
+    lib = _lib.load()
+    header = open(os.path.join(ROOT, "include", "updes_gb300.h")).read()
+    declared = set(re.findall(r"UPDES_API\s+[\w\s\*]+?\b(updes_\w+)\s*\(", header))
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(_lib.SIGNATURES), declared ^ set(_lib.SIGNATURES)
+    assert lib.updes_version() >= 100
+    assert lib.updes_status_string(_lib.ERR_SINGULAR).decode().startswith("singular")
+    assert lib.updes_matrix_ld(22506, 8) == 22528
+
+
+def test_invalid_arguments_rejected_without_gpu():
+    """Argument validation runs before any CUDA call."""
+    lib = _lib.load()
+    p = _lib.Problem()
+    p.N, p.Ni, p.M = 10, 4, 7  # invalid monomial count
+    assert lib.updes_assemble(ctypes.byref(p), None, 0, None, 0, None) == _lib.ERR_INVALID
+    nb = ctypes.c_size_t()
+    assert lib.updes_lu_workspace(0, 0, ctypes.byref(nb)) == _lib.ERR_INVALID
+    assert lib.updes_lu_workspace(100, 5, ctypes.byref(nb)) == _lib.ERR_INVALID
+    assert lib.updes_lu_workspace(100, 1, ctypes.byref(nb)) == _lib.OK and nb.value > 0

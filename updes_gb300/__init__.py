@@ -1,0 +1,18 @@
+"""updes_gb300 — GB300-native global RBF collocation (drop-in for Updes' pde_solver).
+
+Public names follow the reference package (updes 1.0.3): clouds, RBFs, nodal
+operators, field operators and ``pde_solver`` / ``pde_solver_jit`` returning
+``SteadySol(vals, coeffs, mat)``.  Solves run on one GPU through the CUDA
+library built by ``updes_gb300/build.py`` (``python -c "import __graft_entry__ as g; g.build()"``).
+"""
+from .cloud import Cloud, SquareCloud
+from .operators import (
+    DEFAULT_OPTIONS, LAST_INFO, CollocationMatrix, SolverOptions, SteadySol, boundary_conditions_func_to_arr,
+    capture_operator, compute_coefficients, compute_nb_monomials, core_compute_coefficients, divergence,
+    get_field_coefficients, gradient, gradient_vec, laplacian, laplacian_vec, make_all_monomials, make_monomial,
+    nodal_div_grad, nodal_gradient, nodal_laplacian, nodal_value, pde_solver, pde_solver_jit,
+    pde_solver_jit_with_bc, value, value_vec,
+)
+from .rbf import distance, gaussian, inverse_multiquadric, multiquadric, polyharmonic, rbf_spec, thin_plate
+
+__version__ = "0.1.0"

@@ -1,0 +1,371 @@
+// Collocation-matrix assembly and field evaluation kernels (FP64 arithmetic).
+//
+// updes_assemble replaces assemble_op_Phi_P / assemble_bd_Phi_P / the P^T
+// block of assemble_A (updes/assembly.py:93-362, 62-85); updes_eval_values
+// evaluates vals = [Phi P] c (updes/assembly.py:404-410 read backwards).
+#include "common.cuh"
+#include "rbf.cuh"
+#include "stats.cuh"
+
+namespace {
+
+constexpr int kAsmRowsPerWarp = 8;
+constexpr int kAsmWarps = 8;
+constexpr int kAsmRows = kAsmRowsPerWarp * kAsmWarps;  // 64 rows per CTA
+constexpr int kAsmCols = 128;                          // 32 lanes x 4 columns
+
+struct RowInfo {
+  int kind;  // -1 interior, -2 P^T row, else UPDES_ROW_*
+  int a, b;  // evaluation node, partner node
+  double xa, ya, xb, yb;
+  double w0, w1, w2, w3, w4;  // interior: value, d/dx, d/dy, d2/dx2, d2/dy2
+  double n1x, n1y, n2x, n2y, nPx, nPy, beta;
+};
+
+__device__ __forceinline__ RowInfo load_row(const updes_problem& p, int r) {
+  RowInfo ri;
+  if (r < p.Ni) {
+    ri.kind = -1;
+    ri.a = ri.b = r;
+    const double* w = p.op_weights + 5ll * r;
+    ri.w0 = w[0]; ri.w1 = w[1]; ri.w2 = w[2]; ri.w3 = w[3]; ri.w4 = w[4];
+    ri.n1x = ri.n1y = ri.n2x = ri.n2y = ri.nPx = ri.nPy = ri.beta = 0.0;
+  } else if (r < p.N) {
+    const int b = r - p.Ni;
+    ri.kind = p.bd_kind[b];
+    ri.a = p.bd_node[2 * b];
+    ri.b = p.bd_node[2 * b + 1];
+    const double* g = p.bd_geom + 8ll * b;
+    ri.n1x = g[0]; ri.n1y = g[1]; ri.n2x = g[2]; ri.n2y = g[3];
+    ri.nPx = g[4]; ri.nPy = g[5]; ri.beta = g[6];
+    ri.w0 = ri.w1 = ri.w2 = ri.w3 = ri.w4 = 0.0;
+  } else {
+    ri.kind = -2;
+    ri.a = ri.b = r - p.N;  // monomial id
+    ri.w0 = ri.w1 = ri.w2 = ri.w3 = ri.w4 = 0.0;
+    ri.n1x = ri.n1y = ri.n2x = ri.n2y = ri.nPx = ri.nPy = ri.beta = 0.0;
+    ri.xa = ri.ya = ri.xb = ri.yb = 0.0;
+    return ri;
+  }
+  ri.xa = p.nodes[2ll * ri.a];
+  ri.ya = p.nodes[2ll * ri.a + 1];
+  ri.xb = p.nodes[2ll * ri.b];
+  ri.yb = p.nodes[2ll * ri.b + 1];
+  return ri;
+}
+
+// Entry (row, node column c) of K for c < N.
+template <int KIND>
+__device__ __forceinline__ double entry_rbf(const RowInfo& ri, int c, double xc, double yc, double param,
+                                            int ip, int self_term) {
+  if (ri.kind == -2) {  // P^T row: monomial(ri.a) at node c
+    const MonoT m = monomial_terms(ri.a, xc, yc);
+    return m.m;
+  }
+  const double dx = ri.xa - xc, dy = ri.ya - yc;
+  const double r2 = dx * dx + dy * dy;
+  if (ri.kind == -1) {
+    if (c == ri.a && !self_term) return 0.0;
+    if (r2 == 0.0) return ri.w0 * rbf_phi0<KIND>();
+    const RbfG g = rbf_g<KIND>(r2, param, ip);
+    return ri.w0 * g.phi + g.g1 * (ri.w1 * dx + ri.w2 * dy + (ri.w3 + ri.w4)) +
+           g.g2 * (ri.w3 * dx * dx + ri.w4 * dy * dy);
+  }
+  if (ri.kind <= UPDES_ROW_ROBIN) {
+    if (c == ri.a && !self_term) return 0.0;
+    if (r2 == 0.0) return (ri.kind == UPDES_ROW_NEUMANN) ? 0.0 : (ri.kind == UPDES_ROW_ROBIN ? ri.beta : 1.0) * rbf_phi0<KIND>();
+    const RbfG g = rbf_g<KIND>(r2, param, ip);
+    if (ri.kind == UPDES_ROW_DIRICHLET) return g.phi;
+    const double fl = g.g1 * (ri.n1x * dx + ri.n1y * dy);
+    if (ri.kind == UPDES_ROW_NEUMANN) return fl;
+    return ri.beta * g.phi + fl;
+  }
+  // periodic rows span every column
+  const double ex = ri.xb - xc, ey = ri.yb - yc;
+  const double s2 = ex * ex + ey * ey;
+  RbfG ga, gb;
+  if (r2 == 0.0) { ga.phi = rbf_phi0<KIND>(); ga.g1 = 0.0; ga.g2 = 0.0; } else ga = rbf_g<KIND>(r2, param, ip);
+  if (s2 == 0.0) { gb.phi = rbf_phi0<KIND>(); gb.g1 = 0.0; gb.g2 = 0.0; } else gb = rbf_g<KIND>(s2, param, ip);
+  if (ri.kind == UPDES_ROW_PERIODIC_VALUE) return ga.phi - gb.phi;
+  return ga.g1 * (ri.n1x * dx + ri.n1y * dy) + gb.g1 * (ri.n2x * ex + ri.n2y * ey);
+}
+
+// Entry (row, monomial column k) of K.
+__device__ __forceinline__ double entry_mono(const RowInfo& ri, int k) {
+  if (ri.kind == -2) return 0.0;
+  const MonoT m = monomial_terms(k, ri.xa, ri.ya);
+  switch (ri.kind) {
+    case -1:
+      return ri.w0 * m.m + ri.w1 * m.mx + ri.w2 * m.my + ri.w3 * m.mxx + ri.w4 * m.myy;
+    case UPDES_ROW_DIRICHLET:
+      return m.m;
+    case UPDES_ROW_NEUMANN:
+      return m.mx * ri.nPx + m.my * ri.nPy;
+    case UPDES_ROW_ROBIN:
+      return ri.beta * m.m + (m.mx * ri.nPx + m.my * ri.nPy);
+    case UPDES_ROW_PERIODIC_VALUE: {
+      const MonoT q = monomial_terms(k, ri.xb, ri.yb);
+      return m.m - q.m;
+    }
+    default: {
+      const MonoT q = monomial_terms(k, ri.xb, ri.yb);
+      return (m.mx * ri.n1x + m.my * ri.n1y) + (q.mx * ri.n2x + q.my * ri.n2y);
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) assemble_kernel(updes_problem p, int n, double* __restrict__ K64,
+                                                       int64_t ld64, float* __restrict__ K32, int64_t ld32,
+                                                       int64_t ncols) {
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int64_t c0 = int64_t(blockIdx.x) * kAsmCols + 4 * lane;
+  if (c0 >= ncols) return;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const double param = p.rbf_param;
+  double xc[4], yc[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int64_t c = c0 + u;
+    if (c < p.N) {
+      xc[u] = p.nodes[2 * c];
+      yc[u] = p.nodes[2 * c + 1];
+    } else {
+      xc[u] = yc[u] = 0.0;
+    }
+  }
+  const int rbase = blockIdx.y * kAsmRows + warp * kAsmRowsPerWarp;
+  for (int i = 0; i < kAsmRowsPerWarp; ++i) {
+    const int r = rbase + i;
+    if (r >= n) break;
+    const RowInfo ri = load_row(p, r);
+    double v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t c = c0 + u;
+      if (c < p.N) v[u] = entry_rbf<KIND>(ri, int(c), xc[u], yc[u], param, ip, p.self_term);
+      else if (c < n) v[u] = entry_mono(ri, int(c - p.N));
+      else v[u] = 0.0;
+    }
+    if (K64) {
+      double* dst = K64 + int64_t(r) * ld64 + c0;
+      if (c0 + 3 < ncols) {
+        reinterpret_cast<double2*>(dst)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2*>(dst)[1] = make_double2(v[2], v[3]);
+      } else {
+        for (int u = 0; u < 4 && c0 + u < ncols; ++u) dst[u] = v[u];
+      }
+    }
+    if (K32) {
+      float* dst = K32 + int64_t(r) * ld32 + c0;
+      if (c0 + 3 < ncols) {
+        *reinterpret_cast<float4*>(dst) = make_float4(float(v[0]), float(v[1]), float(v[2]), float(v[3]));
+      } else {
+        for (int u = 0; u < 4 && c0 + u < ncols; ++u) dst[u] = float(v[u]);
+      }
+    }
+  }
+}
+
+// vals[i] = sum_{j != i} phi(x_i - x_j) c_j + sum_k m_k(x_i) c_{N+k}
+constexpr int kEvalRows = 16;     // rows per CTA (2 per warp)
+constexpr int kEvalChunk = 512;   // columns staged per pass
+
+template <int KIND>
+__global__ void __launch_bounds__(256) eval_values_kernel(updes_problem p, const double* __restrict__ coeffs,
+                                                          double* __restrict__ vals) {
+  __shared__ double sx[kEvalChunk], sy[kEvalChunk], sc[kEvalChunk];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int r0 = blockIdx.x * kEvalRows + warp * 2;
+  double xi[2], yi[2], acc[2] = {0.0, 0.0};
+  for (int u = 0; u < 2; ++u) {
+    const int r = min(r0 + u, p.N - 1);
+    xi[u] = p.nodes[2 * r];
+    yi[u] = p.nodes[2 * r + 1];
+  }
+  for (int base = 0; base < p.N; base += kEvalChunk) {
+    __syncthreads();
+    for (int t = tid; t < kEvalChunk; t += blockDim.x) {
+      const int c = base + t;
+      if (c < p.N) {
+        sx[t] = p.nodes[2 * c];
+        sy[t] = p.nodes[2 * c + 1];
+        sc[t] = coeffs[c];
+      } else {
+        sx[t] = sy[t] = sc[t] = 0.0;
+      }
+    }
+    __syncthreads();
+    const int lim = min(kEvalChunk, p.N - base);
+    for (int t = lane; t < lim; t += 32) {
+      const int c = base + t;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (c == r0 + u && !p.self_term) continue;
+        acc[u] += rbf_value<KIND>(xi[u] - sx[t], yi[u] - sy[t], p.rbf_param, ip) * sc[t];
+      }
+    }
+  }
+  for (int u = 0; u < 2; ++u) {
+    double a = acc[u];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    acc[u] = a;
+  }
+  if (lane < 2) {
+    const int r = r0 + lane;
+    if (r < p.N) {
+      double s = acc[lane];
+      for (int k = 0; k < p.M; ++k) s += monomial_terms(k, xi[lane], yi[lane]).m * coeffs[p.N + k];
+      vals[r] = s;
+    }
+  }
+}
+
+// Field at arbitrary points from coefficients, summing over every center
+// (updes/operators.py:118-184 value / gradient, :319-348 laplacian).
+// what: 0 value (out m), 1 gradient (out m x 2), 2 laplacian (out m).
+template <int KIND>
+__global__ void __launch_bounds__(256) eval_field_kernel(int m, const double* __restrict__ pts, int N,
+                                                         const double* __restrict__ ctr, int M, double param,
+                                                         const double* __restrict__ coeffs, int what,
+                                                         double* __restrict__ out) {
+  __shared__ double sx[kEvalChunk], sy[kEvalChunk], sc[kEvalChunk];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(param) + 1 : int(param);
+  const int r0 = blockIdx.x * kEvalRows + warp * 2;
+  double xi[2], yi[2], a0[2] = {0.0, 0.0}, a1[2] = {0.0, 0.0};
+  for (int u = 0; u < 2; ++u) {
+    const int r = min(r0 + u, m - 1);
+    xi[u] = pts[2 * r];
+    yi[u] = pts[2 * r + 1];
+  }
+  for (int base = 0; base < N; base += kEvalChunk) {
+    __syncthreads();
+    for (int t = tid; t < kEvalChunk; t += blockDim.x) {
+      const int c = base + t;
+      if (c < N) { sx[t] = ctr[2 * c]; sy[t] = ctr[2 * c + 1]; sc[t] = coeffs[c]; }
+      else { sx[t] = sy[t] = sc[t] = 0.0; }
+    }
+    __syncthreads();
+    const int lim = min(kEvalChunk, N - base);
+    for (int t = lane; t < lim; t += 32) {
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const double dx = xi[u] - sx[t], dy = yi[u] - sy[t];
+        if (what == 0) {
+          a0[u] += rbf_value<KIND>(dx, dy, param, ip) * sc[t];
+        } else {
+          const double r2 = dx * dx + dy * dy;
+          if (r2 == 0.0) continue;
+          const RbfG g = rbf_g<KIND>(r2, param, ip);
+          if (what == 1) { a0[u] += g.g1 * dx * sc[t]; a1[u] += g.g1 * dy * sc[t]; }
+          else a0[u] += (2.0 * g.g1 + g.g2 * r2) * sc[t];
+        }
+      }
+    }
+  }
+  for (int u = 0; u < 2; ++u)
+    for (int o = 16; o > 0; o >>= 1) {
+      a0[u] += __shfl_xor_sync(0xffffffffu, a0[u], o);
+      a1[u] += __shfl_xor_sync(0xffffffffu, a1[u], o);
+    }
+  if (lane < 2) {
+    const int r = r0 + lane;
+    if (r < m) {
+      double v0 = a0[lane], v1 = a1[lane];
+      for (int k = 0; k < M; ++k) {
+        const MonoT mt = monomial_terms(k, xi[lane], yi[lane]);
+        const double gk = coeffs[N + k];
+        if (what == 0) v0 += gk * mt.m;
+        else if (what == 1) { v0 += gk * mt.mx; v1 += gk * mt.my; }
+        else v0 += gk * (mt.mxx + mt.myy);
+      }
+      if (what == 1) { out[2 * r] = v0; out[2 * r + 1] = v1; }
+      else out[r] = v0;
+    }
+  }
+}
+
+int check_problem(const updes_problem* p) {
+  if (!p || p->N <= 0 || p->Ni < 0 || p->Ni > p->N) return UPDES_ERR_INVALID;
+  if (!(p->M == 1 || p->M == 3 || p->M == 6 || p->M == 10 || p->M == 15)) return UPDES_ERR_INVALID;
+  if (p->rbf < 0 || p->rbf > UPDES_RBF_THIN_PLATE) return UPDES_ERR_INVALID;
+  if ((p->rbf == UPDES_RBF_POLYHARMONIC || p->rbf == UPDES_RBF_THIN_PLATE) &&
+      (p->rbf_param < 1.0 || p->rbf_param > 8.0 || p->rbf_param != double(int(p->rbf_param))))
+    return UPDES_ERR_INVALID;
+  if (!p->nodes) return UPDES_ERR_INVALID;
+  if (p->Ni > 0 && !p->op_weights) return UPDES_ERR_INVALID;
+  if (p->N > p->Ni && (!p->bd_kind || !p->bd_node || !p->bd_geom)) return UPDES_ERR_INVALID;
+  return UPDES_OK;
+}
+
+}  // namespace
+
+int updes_check_problem(const updes_problem* p) { return check_problem(p); }
+
+extern "C" int updes_assemble(const updes_problem* p, double* K64, int64_t ld64, float* K32, int64_t ld32,
+                              void* stream) {
+  int st = check_problem(p);
+  if (st) return st;
+  const int n = p->N + p->M;
+  if (!K64 && !K32) return UPDES_ERR_INVALID;
+  if ((K64 && (ld64 < n || ld64 % 2)) || (K32 && (ld32 < n || ld32 % 4))) return UPDES_ERR_INVALID;
+  if ((K64 && (reinterpret_cast<uintptr_t>(K64) & 15)) || (K32 && (reinterpret_cast<uintptr_t>(K32) & 15)))
+    return UPDES_ERR_INVALID;
+  const int64_t ncols = K64 ? (K32 ? (ld64 < ld32 ? ld64 : ld32) : ld64) : ld32;
+  dim3 block(32, kAsmWarps);
+  dim3 grid(unsigned(ceil_div(ncols, kAsmCols)), unsigned(ceil_div(n, kAsmRows)));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  StatScope sc(kStatAssemble, s, 0.0, double(n) * ncols * ((K64 ? 8.0 : 0.0) + (K32 ? 4.0 : 0.0)));
+  switch (p->rbf) {
+    case UPDES_RBF_POLYHARMONIC:
+      assemble_kernel<UPDES_RBF_POLYHARMONIC><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
+    case UPDES_RBF_GAUSSIAN:
+      assemble_kernel<UPDES_RBF_GAUSSIAN><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
+    case UPDES_RBF_MULTIQUADRIC:
+      assemble_kernel<UPDES_RBF_MULTIQUADRIC><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC:
+      assemble_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
+    default:
+      assemble_kernel<UPDES_RBF_THIN_PLATE><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
+  }
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+extern "C" int updes_eval_values(const updes_problem* p, const double* coeffs, double* vals, void* stream) {
+  int st = check_problem(p);
+  if (st) return st;
+  if (!coeffs || !vals) return UPDES_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const unsigned grid = unsigned(ceil_div(p->N, kEvalRows));
+  switch (p->rbf) {
+    case UPDES_RBF_POLYHARMONIC: eval_values_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, coeffs, vals); break;
+    case UPDES_RBF_GAUSSIAN: eval_values_kernel<UPDES_RBF_GAUSSIAN><<<grid, 256, 0, s>>>(*p, coeffs, vals); break;
+    case UPDES_RBF_MULTIQUADRIC: eval_values_kernel<UPDES_RBF_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, coeffs, vals); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC: eval_values_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, coeffs, vals); break;
+    default: eval_values_kernel<UPDES_RBF_THIN_PLATE><<<grid, 256, 0, s>>>(*p, coeffs, vals); break;
+  }
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+extern "C" int updes_eval_field(int32_t m, const double* points, int32_t N, const double* centers, int32_t M,
+                                int32_t rbf, double rbf_param, const double* coeffs, int32_t what, double* out,
+                                void* stream) {
+  if (m <= 0 || N <= 0 || !points || !centers || !coeffs || !out || what < 0 || what > 2) return UPDES_ERR_INVALID;
+  if (!(M == 0 || M == 1 || M == 3 || M == 6 || M == 10 || M == 15)) return UPDES_ERR_INVALID;
+  if (rbf < 0 || rbf > UPDES_RBF_THIN_PLATE) return UPDES_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const unsigned grid = unsigned(ceil_div(m, kEvalRows));
+  switch (rbf) {
+    case UPDES_RBF_POLYHARMONIC: eval_field_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
+    case UPDES_RBF_GAUSSIAN: eval_field_kernel<UPDES_RBF_GAUSSIAN><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
+    case UPDES_RBF_MULTIQUADRIC: eval_field_kernel<UPDES_RBF_MULTIQUADRIC><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC: eval_field_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
+    default: eval_field_kernel<UPDES_RBF_THIN_PLATE><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
+  }
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}

@@ -1,0 +1,81 @@
+// Shared helpers for the updes_gb300 CUDA sources (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/updes_gb300.h"
+
+#define UPDES_CUDA_TRY(expr)                                   \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if (_e != cudaSuccess) {                                   \
+      updes_set_last_cuda_error(_e, #expr, __FILE__, __LINE__); \
+      return UPDES_ERR_CUDA;                                   \
+    }                                                          \
+  } while (0)
+
+void stats_count_launch(int n);
+#define UPDES_LAUNCH_CHECK()          \
+  do {                                \
+    stats_count_launch(1);            \
+    UPDES_CUDA_TRY(cudaGetLastError()); \
+  } while (0)
+
+// Records the last CUDA error (text retrievable through updes_last_error()).
+void updes_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+
+// Device-side status word layout (written by kernels, read by the host after a sync).
+// word 0: first error code (UPDES_ERR_*) raised by any kernel, 0 if none
+// word 1: LU info (1 + first step with a zero / non-finite pivot), 0 if none
+// word 2: where a bounded wait gave up (kernel-specific tag)
+struct DeviceStatus {
+  int32_t error;
+  int32_t lu_info;
+  int32_t timeout_tag;
+  int32_t pad;
+};
+
+__device__ __forceinline__ void status_error(DeviceStatus* st, int code) {
+  atomicCAS(&st->error, 0, code);
+}
+
+__host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Iteration cap of every spin-wait (each iteration also sleeps ~64 ns): a few seconds at most.
+constexpr long long kSpinLimit = 1ll << 26;
+
+// Grid-wide barrier for a cooperative launch (all CTAs co-resident).
+// `bar` points at two words: arrival count and generation.  Returns false if
+// the wait gave up (the caller must then stop and report UPDES_ERR_TIMEOUT).
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int nblocks, DeviceStatus* st,
+                                             int tag) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned int* vgen = bar + 1;
+    unsigned int gen = *vgen;
+    __threadfence();
+    unsigned int ticket = atomicAdd(bar, 1u);
+    if (ticket == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long it = 0;
+      while (*vgen == gen) {
+        if (++it > kSpinLimit) {
+          ok = 0;
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, tag);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}

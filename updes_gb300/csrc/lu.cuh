@@ -1,0 +1,22 @@
+// Internal interface of the LU and triangular-solve kernels.
+#pragma once
+
+#include "common.cuh"
+
+constexpr int kLuNb = 64;  // panel width
+
+// Optional replacement of the trailing update W[k+nb:, k+nb:] -= F21 * F12.
+struct LuHooks {
+  void* ctx;
+  int (*gemm)(void* ctx, int n, int k, int nb, double* W, int64_t ldw, const void* F, int64_t ldf, cudaStream_t s);
+};
+
+size_t lu_panel_workspace_bytes(int nb);
+
+template <typename TF>
+int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* piv, void* ws, size_t ws_bytes,
+                   DeviceStatus* st, cudaStream_t s, const LuHooks* hooks);
+
+// mode: 0 = L, 1 = U, 2 = U^T, 3 = L^T (x overwritten in place); sync_ws: ceil(n/64)+1 ints.
+template <typename TF>
+int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s);

@@ -1,0 +1,756 @@
+// Public LU / solve entry points and the GMRES-refined collocation solve.
+//
+// updes_solve replaces pde_solver's assemble_B -> lineax QR ->
+// core_compute_coefficients sequence (updes/operators.py:602-618) by one
+// factorisation of the augmented Kansa matrix K and refinement in FP64.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "gemm_tc.cuh"
+#include "lu.cuh"
+#include "stats.cuh"
+
+int updes_check_problem(const updes_problem* p);
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_last_error;
+
+constexpr int kMaxPermN = 51200;  // permutation built in shared memory
+
+__global__ void perm_from_piv_kernel(const int32_t* __restrict__ piv, int n, int32_t* __restrict__ perm) {
+  extern __shared__ int32_t sp[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) {
+      const int p = piv[i];
+      if (p != i) {
+        const int a = sp[i];
+        sp[i] = sp[p];
+        sp[p] = a;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
+}
+
+// out[i] = scale[i] * in[perm[i]] (gather, scale may be null) or out[perm[i]] = in[i] (scatter)
+__global__ void permute_kernel(double* __restrict__ out, const double* __restrict__ in, int64_t in_stride,
+                               int64_t out_stride, const int32_t* __restrict__ perm, int n, int scatter) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (scatter) out[int64_t(perm[i]) * out_stride] = in[int64_t(i) * in_stride];
+  else out[int64_t(i) * out_stride] = in[int64_t(perm[i]) * in_stride];
+}
+
+// dr[i] = 2^-round(log2(max_j |K_ij|)) (power of two, so scaling is exact)
+__global__ void row_scale_kernel(const double* __restrict__ K, int64_t ld, int n, double* __restrict__ dr) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  double m = 0.0;
+  for (int j = lane; j < n; j += 32) m = fmax(m, fabs(K[int64_t(warp) * ld + j]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) {
+    int e = 0;
+    if (m > 0.0 && isfinite(m)) frexp(m, &e);
+    dr[warp] = ldexp(1.0, -e);
+  }
+}
+
+__global__ void col_scale_kernel(const double* __restrict__ K, int64_t ld, int n, const double* __restrict__ dr,
+                                 double* __restrict__ dc) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double m = 0.0;
+  for (int i = 0; i < n; ++i) m = fmax(m, fabs(K[int64_t(i) * ld + j]) * dr[i]);
+  int e = 0;
+  if (m > 0.0 && isfinite(m)) frexp(m, &e);
+  dc[j] = ldexp(1.0, -e);
+}
+
+__global__ void scale_copy_kernel(const double* __restrict__ K, int64_t ldk, double* __restrict__ W, int64_t ldw,
+                                  int n, const double* __restrict__ dr, const double* __restrict__ dc) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t i = e / ldw, j = e % ldw;
+  if (i >= n) return;
+  W[i * ldw + j] = (j < n) ? dr[i] * K[i * ldk + j] * dc[j] : 0.0;
+}
+
+// out_i = dr_i * (bsign * b_i + ksign * sum_j K_ij dc_j x_j), one warp per row (dr, dc, b may be null)
+// With absout != null also writes absout_i = dr_i * (sum_j |K_ij dc_j x_j| + |b_i|) (backward-error denominators).
+__global__ void __launch_bounds__(256) gemv_kernel(const double* __restrict__ K, int64_t ld, int n,
+                                                   const double* __restrict__ x, const double* __restrict__ b,
+                                                   const double* __restrict__ dr, const double* __restrict__ dc,
+                                                   double bsign, double ksign, double* __restrict__ out,
+                                                   double* __restrict__ absout = nullptr) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* row = K + int64_t(warp) * ld;
+  double s = 0.0, a = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    const double t = row[j] * (dc ? dc[j] * x[j] : x[j]);
+    s += t;
+    a += fabs(t);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+  }
+  if (lane == 0) {
+    double v = ksign * s + (b ? bsign * b[warp] : 0.0);
+    out[warp] = dr ? dr[warp] * v : v;
+    if (absout) absout[warp] = (dr ? dr[warp] : 1.0) * (a + (b ? fabs(b[warp]) : 0.0));
+  }
+}
+
+// partial maxima of |r_i| / a_i (a_i = 0 with r_i = 0 counts as 0)
+__global__ void bwd_partial_kernel(const double* __restrict__ r, const double* __restrict__ a, int n,
+                                   double* __restrict__ partial) {
+  __shared__ double red[8];
+  double m = 0.0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const double rr = fabs(r[t]);
+    const double v = a[t] > 0.0 ? rr / a[t] : (rr > 0.0 ? INFINITY : 0.0);
+    m = fmax(m, v != v ? INFINITY : v);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t = fmax(t, red[q]);
+    partial[blockIdx.x] = t;
+  }
+}
+
+// Transposed: out_j = dc_j * (bsign * b_j + ksign * sum_i K_ij dr_i x_i), 256 columns per CTA.
+__global__ void __launch_bounds__(256) gemv_t_kernel(const double* __restrict__ K, int64_t ld, int n,
+                                                     const double* __restrict__ x, const double* __restrict__ b,
+                                                     const double* __restrict__ dr, const double* __restrict__ dc,
+                                                     double bsign, double ksign, double* __restrict__ out) {
+  __shared__ double part[8][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  double s = 0.0;
+  if (j < n)
+    for (int i = w; i < n; i += 8) s = fma(K[int64_t(i) * ld + j], dr ? dr[i] * x[i] : x[i], s);
+  part[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && j < n) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t += part[q][lane];
+    double v = ksign * t + (b ? bsign * b[j] : 0.0);
+    out[j] = dc ? dc[j] * v : v;
+  }
+}
+
+constexpr int kDotBlocks = 120;
+constexpr double kBwdFloor = 64.0 * 1.1102230246251565e-16;  // 64 unit roundoffs of FP64
+
+// partial[b * nv + i] = sum over block b's chunk of V_i . w
+__global__ void __launch_bounds__(256) multi_dot_kernel(const double* __restrict__ V, int64_t ldv, int nv,
+                                                        const double* __restrict__ w, int n,
+                                                        double* __restrict__ partial) {
+  __shared__ double red[8];
+  const int chunk = int(ceil_div(n, gridDim.x));
+  const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  for (int i = 0; i < nv; ++i) {
+    double s = 0.0;
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) s = fma(V[int64_t(i) * ldv + t], w[t], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int q = 0; q < 8; ++q) t += red[q];
+      partial[blockIdx.x * nv + i] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void reduce_partials_kernel(const double* __restrict__ partial, int nblocks, int nv, double* __restrict__ h) {
+  const int i = threadIdx.x;
+  if (i >= nv) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += partial[b * nv + i];
+  h[i] = s;
+}
+
+// w += sign * sum_i h_i V_i ; if out != null writes there instead of w (out = sign * sum_i h_i V_i)
+__global__ void multi_axpy_kernel(const double* __restrict__ V, int64_t ldv, int nv, const double* __restrict__ h,
+                                  double sign, double* __restrict__ w, double* __restrict__ out, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double s = 0.0;
+  for (int i = 0; i < nv; ++i) s = fma(h[i], V[int64_t(i) * ldv + t], s);
+  if (out) out[t] = sign * s;
+  else w[t] += sign * s;
+}
+
+__global__ void axpby_kernel(double* y, double a, const double* x, double b, int n,
+                             const double* __restrict__ mul) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double v = a * x[t] + b * y[t];
+  y[t] = mul ? v * mul[t] : v;
+}
+
+__global__ void rhs_kernel(const double* __restrict__ q, int N, int n, const double* __restrict__ dr,
+                           double* __restrict__ bs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  bs[t] = (t < N ? q[t] : 0.0) * dr[t];
+}
+
+__global__ void abs_kernel(const double* __restrict__ x, double* __restrict__ y, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = fabs(x[t]);
+}
+
+struct Carve {
+  char* base;
+  size_t off = 0;
+  template <typename T>
+  T* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+}  // namespace
+
+void updes_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  char buf[512];
+  snprintf(buf, sizeof buf, "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+  g_last_error = buf;
+}
+
+extern "C" const char* updes_last_error(void) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  static thread_local std::string copy;
+  copy = g_last_error;
+  return copy.c_str();
+}
+
+extern "C" int updes_version(void) { return 100; }
+
+extern "C" const char* updes_status_string(int status) {
+  switch (status) {
+    case UPDES_OK: return "ok";
+    case UPDES_ERR_INVALID: return "invalid argument";
+    case UPDES_ERR_CUDA: return "CUDA runtime error";
+    case UPDES_ERR_SINGULAR: return "singular matrix (zero or non-finite pivot)";
+    case UPDES_ERR_NOT_CONVERGED: return "iterative refinement did not converge";
+    case UPDES_ERR_TIMEOUT: return "a bounded device-side wait timed out";
+    case UPDES_ERR_UNSUPPORTED: return "unsupported by this build";
+    case UPDES_ERR_WORKSPACE: return "workspace too small";
+    default: return "unknown status";
+  }
+}
+
+extern "C" int64_t updes_matrix_ld(int64_t n, int32_t elem_bytes) {
+  (void)elem_bytes;
+  return (n + 31) / 32 * 32;
+}
+
+// ---------------------------------------------------------------------------
+// LU entry points
+// ---------------------------------------------------------------------------
+namespace {
+
+struct LuWs {
+  DeviceStatus* st;
+  void* panel;
+  size_t panel_bytes;
+  int* sync;
+  double* tmp;
+  void* gemm_ws;
+  size_t gemm_bytes;
+};
+
+size_t lu_ws_layout(int n, int precision, char* base, LuWs* out) {
+  Carve c{base};
+  LuWs w;
+  w.st = c.take<DeviceStatus>(1);
+  w.panel_bytes = lu_panel_workspace_bytes(kLuNb);
+  w.panel = c.take<char>(w.panel_bytes);
+  w.sync = c.take<int>(ceil_div(n, 64) + 2);
+  w.tmp = c.take<double>(n);
+  w.gemm_bytes = (precision == UPDES_PREC_FP32) ? gemm_tc_workspace_bytes(n) : 0;
+  w.gemm_ws = c.take<char>(w.gemm_bytes);
+  if (out) *out = w;
+  return c.off + 256;
+}
+
+int read_status(DeviceStatus* st, cudaStream_t s, DeviceStatus* host) {
+  UPDES_CUDA_TRY(cudaMemcpyAsync(host, st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+  UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+  return UPDES_OK;
+}
+
+int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t ldf, int32_t* piv, const LuWs& w,
+                cudaStream_t s) {
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DeviceStatus), s));
+  int e;
+  if (precision == UPDES_PREC_FP64) {
+    double* Fd = F ? static_cast<double*>(F) : A;
+    if (Fd != A) {
+      UPDES_CUDA_TRY(cudaMemcpy2DAsync(Fd, ldf * 8, A, lda * 8, size_t(n) * 8, n, cudaMemcpyDeviceToDevice, s));
+      A = Fd;
+      lda = ldf;
+    }
+    e = lu_factor_impl<double>(n, A, lda, A, lda, piv, w.panel, w.panel_bytes, w.st, s, nullptr);
+  } else {
+    GemmTcCtx ctx{w.gemm_ws, w.gemm_bytes};
+    LuHooks hooks{&ctx, gemm_tc_update};
+    e = lu_factor_impl<float>(n, A, lda, static_cast<float*>(F), ldf, piv, w.panel, w.panel_bytes, w.st, s,
+                              gemm_tc_enabled() ? &hooks : nullptr);
+  }
+  if (e) return e;
+  if (n > kMaxPermN) return UPDES_ERR_UNSUPPORTED;
+  UPDES_CUDA_TRY(cudaFuncSetAttribute(perm_from_piv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(n * sizeof(int32_t))));
+  perm_from_piv_kernel<<<1, 1024, n * sizeof(int32_t), s>>>(piv, n, piv + n);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+// x (contiguous, n) <- A^-1 x or A^-T x using the permutation in piv[n, 2n)
+template <typename TF>
+int solve_core(int n, const TF* F, int64_t ldf, const int32_t* piv, double* x, int trans, const LuWs& w,
+               cudaStream_t s) {
+  const int32_t* perm = piv + n;
+  const unsigned g = unsigned(ceil_div(n, 256));
+  if (!trans) {
+    permute_kernel<<<g, 256, 0, s>>>(w.tmp, x, 1, 1, perm, n, 0);
+    UPDES_LAUNCH_CHECK();
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s);
+    if (e) return e;
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s);
+    if (e) return e;
+    UPDES_CUDA_TRY(cudaMemcpyAsync(x, w.tmp, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+  } else {
+    UPDES_CUDA_TRY(cudaMemcpyAsync(w.tmp, x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s);
+    if (e) return e;
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s);
+    if (e) return e;
+    permute_kernel<<<g, 256, 0, s>>>(x, w.tmp, 1, 1, perm, n, 1);
+    UPDES_LAUNCH_CHECK();
+  }
+  return UPDES_OK;
+}
+
+int solve_any(int n, const void* F, int64_t ldf, int precision, const int32_t* piv, double* x, int trans,
+              const LuWs& w, cudaStream_t s) {
+  if (precision == UPDES_PREC_FP64) return solve_core<double>(n, static_cast<const double*>(F), ldf, piv, x, trans, w, s);
+  return solve_core<float>(n, static_cast<const float*>(F), ldf, piv, x, trans, w, s);
+}
+
+}  // namespace
+
+extern "C" int updes_lu_workspace(int32_t n, int32_t precision, size_t* bytes) {
+  if (n <= 0 || !bytes || (precision != UPDES_PREC_FP64 && precision != UPDES_PREC_FP32)) return UPDES_ERR_INVALID;
+  *bytes = lu_ws_layout(n, precision, nullptr, nullptr);
+  return UPDES_OK;
+}
+
+extern "C" int updes_lu_factor(int32_t n, double* A, int64_t lda, int32_t precision, void* F, int64_t ldf,
+                               int32_t* piv, void* workspace, size_t workspace_bytes, int32_t* info, void* stream) {
+  if (n <= 0 || !A || lda < n || !piv || !workspace) return UPDES_ERR_INVALID;
+  if (precision != UPDES_PREC_FP64 && precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
+  if (precision == UPDES_PREC_FP32 && (!F || ldf < n)) return UPDES_ERR_INVALID;
+  if (precision == UPDES_PREC_FP64 && F && ldf < n) return UPDES_ERR_INVALID;
+  if (workspace_bytes < lu_ws_layout(n, precision, nullptr, nullptr)) return UPDES_ERR_WORKSPACE;
+  LuWs w;
+  lu_ws_layout(n, precision, static_cast<char*>(workspace), &w);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int e = factor_core(n, A, lda, precision, F, ldf, piv, w, s);
+  if (e) return e;
+  DeviceStatus h;
+  e = read_status(w.st, s, &h);
+  if (e) return e;
+  if (info) *info = h.lu_info;
+  if (h.error) return h.error;
+  return UPDES_OK;
+}
+
+extern "C" int updes_lu_solve(int32_t n, const void* F, int64_t ldf, int32_t precision, const int32_t* piv,
+                              double* b, int32_t nrhs, int64_t ldb, int32_t trans, void* workspace,
+                              size_t workspace_bytes, void* stream) {
+  if (n <= 0 || !F || ldf < n || !piv || !b || nrhs <= 0 || ldb < nrhs || !workspace) return UPDES_ERR_INVALID;
+  if (precision != UPDES_PREC_FP64 && precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
+  if (workspace_bytes < lu_ws_layout(n, precision, nullptr, nullptr) + size_t(n) * 8 + 256) return UPDES_ERR_WORKSPACE;
+  LuWs w;
+  size_t used = lu_ws_layout(n, precision, static_cast<char*>(workspace), &w);
+  double* col = reinterpret_cast<double*>(static_cast<char*>(workspace) + ((used + 255) & ~size_t(255)));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DeviceStatus), s));
+  for (int j = 0; j < nrhs; ++j) {
+    double* bj = b + j;
+    if (nrhs == 1) {
+      int e = solve_any(n, F, ldf, precision, piv, bj, trans, w, s);
+      if (e) return e;
+      continue;
+    }
+    UPDES_CUDA_TRY(cudaMemcpy2DAsync(col, 8, bj, ldb * 8, 8, n, cudaMemcpyDeviceToDevice, s));
+    int e = solve_any(n, F, ldf, precision, piv, col, trans, w, s);
+    if (e) return e;
+    UPDES_CUDA_TRY(cudaMemcpy2DAsync(bj, ldb * 8, col, 8, 8, n, cudaMemcpyDeviceToDevice, s));
+  }
+  DeviceStatus h;
+  int e = read_status(w.st, s, &h);
+  if (e) return e;
+  return h.error;
+}
+
+extern "C" int updes_residual(int32_t n, const double* K, int64_t ldk, const double* x, const double* b, double* r,
+                              int32_t trans, void* stream) {
+  if (n <= 0 || !K || ldk < n || !x || !b || !r) return UPDES_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!trans) gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(K, ldk, n, x, b, nullptr, nullptr, 1.0, -1.0, r);
+  else gemv_t_kernel<<<unsigned(ceil_div(n, 32)), 256, 0, s>>>(K, ldk, n, x, b, nullptr, nullptr, 1.0, -1.0, r);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The full solve
+// ---------------------------------------------------------------------------
+namespace {
+
+struct SolveWs {
+  LuWs lu;
+  double *K64, *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *partial, *h;
+  float* F32;
+  int32_t* piv;
+  int64_t ld;
+};
+
+size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* out) {
+  SolveWs w;
+  const int64_t ld = updes_matrix_ld(n, 8);
+  Carve c{base};
+  const size_t lub = lu_ws_layout(n, o.precision, nullptr, nullptr);
+  char* lubase = c.take<char>(lub);
+  if (base) lu_ws_layout(n, o.precision, lubase, &w.lu);
+  w.ld = ld;
+  w.K64 = c.take<double>(size_t(n) * ld);
+  w.W = c.take<double>(size_t(n) * ld);
+  w.F32 = (o.precision == UPDES_PREC_FP32) ? c.take<float>(size_t(n) * ld) : nullptr;
+  w.piv = c.take<int32_t>(2 * size_t(n));
+  w.dr = c.take<double>(n);
+  w.dc = c.take<double>(n);
+  w.bs = c.take<double>(n);
+  w.bsabs = c.take<double>(n);
+  w.absr = c.take<double>(n);
+  w.x = c.take<double>(n);
+  w.r = c.take<double>(n);
+  w.z = c.take<double>(n);
+  w.wv = c.take<double>(n);
+  const int m = o.restart > 0 ? o.restart : 1;
+  w.V = c.take<double>(size_t(m + 1) * n);
+  w.partial = c.take<double>(size_t(kDotBlocks) * (m + 2));
+  w.h = c.take<double>(m + 2);
+  if (out) *out = w;
+  return c.off + 256;
+}
+
+updes_solve_opts normalise(const updes_solve_opts* o) {
+  updes_solve_opts d;
+  d.precision = UPDES_PREC_FP32;
+  d.max_iters = 200;
+  d.restart = 40;
+  d.fallback_fp64 = 1;
+  d.tol = 1e-13;
+  if (o) {
+    d = *o;
+    if (d.max_iters <= 0) d.max_iters = 200;
+    if (d.restart <= 0) d.restart = 40;
+    if (d.restart > 200) d.restart = 200;
+    if (!(d.tol > 0)) d.tol = 1e-13;
+  }
+  return d;
+}
+
+// h[0..nv) = V[0..nv)^T w (device), then copied to host
+int multi_dot(const double* V, int64_t ldv, int nv, const double* w, int n, double* partial, double* h_dev,
+              double* h_host, cudaStream_t s) {
+  multi_dot_kernel<<<kDotBlocks, 256, 0, s>>>(V, ldv, nv, w, n, partial);
+  UPDES_LAUNCH_CHECK();
+  reduce_partials_kernel<<<1, 256, 0, s>>>(partial, kDotBlocks, nv, h_dev);
+  UPDES_LAUNCH_CHECK();
+  if (h_host) {
+    UPDES_CUDA_TRY(cudaMemcpyAsync(h_host, h_dev, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+    UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return UPDES_OK;
+}
+
+struct Timer {
+  cudaEvent_t a, b;
+  cudaStream_t s;
+  bool ok;
+  explicit Timer(cudaStream_t st) : s(st) {
+    ok = cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess;
+    if (ok) cudaEventRecord(a, s);
+  }
+  double stop() {
+    if (!ok) return 0.0;
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ok = false;
+    return ms;
+  }
+  ~Timer() {
+    if (ok) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  }
+};
+
+// Ks z = dr .* (K (dc .* z))
+int apply_K(const SolveWs& w, int n, const double* z, double* out, cudaStream_t s) {
+  StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * n);
+  gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, z, nullptr, w.dr, w.dc, 0.0,
+                                                                         1.0, out);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+// out = bs - Ks x; also returns (on the host) the componentwise backward error
+// max_i |out_i| / (|Ks| |x| + |bs|)_i.
+int residual_scaled(const SolveWs& w, int n, const double* x, double* out, double* bwd, cudaStream_t s) {
+  StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * n);
+  gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, x, nullptr, w.dr, w.dc, 0.0,
+                                                                         -1.0, out, w.absr);
+  UPDES_LAUNCH_CHECK();
+  axpby_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(out, 1.0, w.bs, 1.0, n, nullptr);
+  UPDES_LAUNCH_CHECK();
+  axpby_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(w.absr, 1.0, w.bsabs, 1.0, n, nullptr);
+  UPDES_LAUNCH_CHECK();
+  bwd_partial_kernel<<<kDotBlocks, 256, 0, s>>>(out, w.absr, n, w.partial);
+  UPDES_LAUNCH_CHECK();
+  std::vector<double> part(kDotBlocks);
+  UPDES_CUDA_TRY(cudaMemcpyAsync(part.data(), w.partial, kDotBlocks * sizeof(double), cudaMemcpyDeviceToHost, s));
+  UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+  double m = 0.0;
+  for (double v : part) m = std::fmax(m, v);
+  *bwd = m;
+  return UPDES_OK;
+}
+
+int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s) {
+  if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, 0, w.lu, s);
+  return solve_core<float>(n, w.F32, w.ld, w.piv, x, 0, w.lu, s);
+}
+
+[[maybe_unused]] double host_norm(const std::vector<double>& v) {
+  double s = 0;
+  for (double a : v) s += a * a;
+  return std::sqrt(s);
+}
+
+// Restarted, right-preconditioned GMRES on Ks x = bs starting from w.x.
+int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, updes_solve_info* info,
+          cudaStream_t s) {
+  const int m = o.restart;
+  const unsigned g = unsigned(ceil_div(n, 256));
+  std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), gv(m + 1), hcol(m + 2);
+  double bnorm2;
+  int e = multi_dot(w.bs, n, 1, w.bs, n, w.partial, w.h, &bnorm2, s);
+  if (e) return e;
+  const double bnorm = std::sqrt(bnorm2);
+  int total = 0, stalls = 0;
+  double last_beta = INFINITY;
+  for (;;) {
+    double bwd;
+    if ((e = residual_scaled(w, n, w.x, w.r, &bwd, s))) return e;
+    double beta2;
+    if ((e = multi_dot(w.r, n, 1, w.r, n, w.partial, w.h, &beta2, s))) return e;
+    const double beta = std::sqrt(beta2);
+    info->rel_residual = bnorm > 0 ? beta / bnorm : beta;
+    info->backward_error = bwd;
+    if (!(beta == beta)) return UPDES_ERR_NOT_CONVERGED;
+    if (beta <= o.tol * bnorm || bwd <= kBwdFloor) {
+      info->converged = 1;
+      break;
+    }
+    if (total >= o.max_iters) break;
+    if (beta > 0.5 * last_beta) {
+      if (++stalls >= 2) break;
+    }
+    last_beta = beta;
+    // V0 = r / beta
+    axpby_kernel<<<g, 256, 0, s>>>(w.V, 1.0 / beta, w.r, 0.0, n, nullptr);
+    UPDES_LAUNCH_CHECK();
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+    int j = 0;
+    for (; j < m && total < o.max_iters; ++j, ++total) {
+      double* vj = w.V + size_t(j) * n;
+      UPDES_CUDA_TRY(cudaMemcpyAsync(w.z, vj, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+      if ((e = precond(w, n, precision, w.z, s))) return e;
+      if ((e = apply_K(w, n, w.z, w.wv, s))) return e;
+      // CGS2
+      std::fill(hcol.begin(), hcol.end(), 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        std::vector<double> hh(j + 1);
+        if ((e = multi_dot(w.V, n, j + 1, w.wv, n, w.partial, w.h, hh.data(), s))) return e;
+        multi_axpy_kernel<<<g, 256, 0, s>>>(w.V, n, j + 1, w.h, -1.0, w.wv, nullptr, n);
+        UPDES_LAUNCH_CHECK();
+        for (int i = 0; i <= j; ++i) hcol[i] += hh[i];
+      }
+      double hn2;
+      if ((e = multi_dot(w.wv, n, 1, w.wv, n, w.partial, w.h, &hn2, s))) return e;
+      const double hn = std::sqrt(hn2);
+      hcol[j + 1] = hn;
+      if (hn > 0) {
+        axpby_kernel<<<g, 256, 0, s>>>(w.V + size_t(j + 1) * n, 1.0 / hn, w.wv, 0.0, n, nullptr);
+        UPDES_LAUNCH_CHECK();
+      }
+      // Givens
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+        hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+        hcol[i] = t;
+      }
+      const double d = std::hypot(hcol[j], hcol[j + 1]);
+      cs[j] = d > 0 ? hcol[j] / d : 1.0;
+      sn[j] = d > 0 ? hcol[j + 1] / d : 0.0;
+      hcol[j] = d;
+      hcol[j + 1] = 0.0;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      for (int i = 0; i <= j; ++i) H[size_t(i) * m + j] = hcol[i];
+      if (std::fabs(gv[j + 1]) <= o.tol * bnorm || hn == 0.0) {
+        ++j;
+        ++total;
+        break;
+      }
+    }
+    // y = R^-1 g
+    std::vector<double> y(j);
+    for (int i = j - 1; i >= 0; --i) {
+      double t = gv[i];
+      for (int k = i + 1; k < j; ++k) t -= H[size_t(i) * m + k] * y[k];
+      y[i] = H[size_t(i) * m + i] != 0 ? t / H[size_t(i) * m + i] : 0.0;
+    }
+    if (j > 0) {
+      UPDES_CUDA_TRY(cudaMemcpyAsync(w.h, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s));
+      multi_axpy_kernel<<<g, 256, 0, s>>>(w.V, n, j, w.h, 1.0, nullptr, w.z, n);
+      UPDES_LAUNCH_CHECK();
+      if ((e = precond(w, n, precision, w.z, s))) return e;
+      axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.z, 1.0, n, nullptr);
+      UPDES_LAUNCH_CHECK();
+      UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+  }
+  if (precision == UPDES_PREC_FP32) info->iters = total;
+  return UPDES_OK;
+}
+
+}  // namespace
+
+extern "C" int updes_solve_workspace(const updes_problem* p, const updes_solve_opts* opts, size_t* bytes) {
+  if (updes_check_problem(p) || !bytes) return UPDES_ERR_INVALID;
+  const updes_solve_opts o = normalise(opts);
+  updes_solve_opts o64 = o;
+  o64.precision = UPDES_PREC_FP32;  // the FP64 fallback fits in the same layout
+  *bytes = solve_ws_layout(p->N + p->M, o64, nullptr, nullptr);
+  return UPDES_OK;
+}
+
+extern "C" int updes_solve(const updes_problem* p, const double* q, double* coeffs, double* vals,
+                           const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+  if (updes_check_problem(p) || !q || !coeffs || !workspace) return UPDES_ERR_INVALID;
+  updes_solve_opts o = normalise(opts);
+  if (o.precision != UPDES_PREC_FP64 && o.precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
+  const int n = p->N + p->M;
+  updes_solve_opts olay = o;
+  olay.precision = UPDES_PREC_FP32;
+  if (workspace_bytes < solve_ws_layout(n, olay, nullptr, nullptr)) return UPDES_ERR_WORKSPACE;
+  SolveWs w;
+  solve_ws_layout(n, olay, static_cast<char*>(workspace), &w);
+  updes_solve_info dummy;
+  if (!info) info = &dummy;
+  std::memset(info, 0, sizeof *info);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const unsigned g = unsigned(ceil_div(n, 256));
+  int e;
+  {
+    Timer t(s);
+    if ((e = updes_assemble(p, w.K64, w.ld, nullptr, 0, stream))) return e;
+    row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, w.dr);
+    UPDES_LAUNCH_CHECK();
+    col_scale_kernel<<<g, 256, 0, s>>>(w.K64, w.ld, n, w.dr, w.dc);
+    UPDES_LAUNCH_CHECK();
+    info->t_assemble_ms = t.stop();
+  }
+  int precision = o.precision;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    {
+      Timer t(s);
+      scale_copy_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.K64, w.ld, w.W, w.ld, n, w.dr, w.dc);
+      UPDES_LAUNCH_CHECK();
+      e = factor_core(n, w.W, w.ld, precision, precision == UPDES_PREC_FP64 ? nullptr : w.F32, w.ld, w.piv, w.lu, s);
+      if (e) return e;
+      DeviceStatus h;
+      if ((e = read_status(w.lu.st, s, &h))) return e;
+      if (h.error) return h.error;
+      info->lu_info = h.lu_info;
+      info->t_factor_ms += t.stop();
+    }
+    Timer t(s);
+    rhs_kernel<<<g, 256, 0, s>>>(q, p->N, n, w.dr, w.bs);
+    UPDES_LAUNCH_CHECK();
+    abs_kernel<<<g, 256, 0, s>>>(w.bs, w.bsabs, n);
+    UPDES_LAUNCH_CHECK();
+    UPDES_CUDA_TRY(cudaMemcpyAsync(w.x, w.bs, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+    if ((e = precond(w, n, precision, w.x, s))) return e;
+    updes_solve_opts oi = o;
+    if (precision == UPDES_PREC_FP64) oi.max_iters = 0;  // plain FP64 LU: report the residual only
+    if ((e = gmres(w, n, precision, oi, info, s))) return e;
+    DeviceStatus h;
+    if ((e = read_status(w.lu.st, s, &h))) return e;
+    if (h.error) return h.error;
+    info->t_refine_ms += t.stop();
+    if (precision == UPDES_PREC_FP64) {
+      info->converged = 1;
+      break;
+    }
+    if (info->converged || !o.fallback_fp64) break;
+    precision = UPDES_PREC_FP64;
+    info->fell_back = 1;
+  }
+  // coeffs = dc .* x
+  {
+    Timer t(s);
+    axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.x, 0.0, n, w.dc);
+    UPDES_LAUNCH_CHECK();
+    UPDES_CUDA_TRY(cudaMemcpyAsync(coeffs, w.x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+    if (vals && (e = updes_eval_values(p, coeffs, vals, stream))) return e;
+    info->t_eval_ms = t.stop();
+  }
+  if (info->lu_info) return UPDES_ERR_SINGULAR;
+  if (!info->converged) return UPDES_ERR_NOT_CONVERGED;
+  return UPDES_OK;
+}
