@@ -201,8 +201,9 @@ def run_ours(args, world, rank, local):
 
     torch.cuda.set_device(local)
     cloud, op, rhs, bcs, ustar = make_problem(args.nx, U)
-    opts32 = SolverOptions(precision="fp32")
-    opts64 = SolverOptions(precision="fp64")
+    # every timed step is a fresh system: no reuse of earlier factors
+    opts32 = SolverOptions(precision="fp32", reuse_factorization=False)
+    opts64 = SolverOptions(precision="fp64", reuse_factorization=False)
     W, kind, bnodes, geom, q = prepare(op, rhs, cloud, bcs, U.polyharmonic, 2, options=opts32)
     dp = DeviceProblem(cloud, U.polyharmonic, 2, W, kind, bnodes, geom)
     qd = torch.as_tensor(q, device="cuda")

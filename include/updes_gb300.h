@@ -204,6 +204,56 @@ UPDES_API int updes_solve(const updes_problem* p, const double* q, double* coeff
                 const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
                 size_t workspace_bytes, void* stream);
 
+/*
+ * Factor once, solve many.  updes_factor assembles, equilibrates and factors K
+ * into `workspace` (layout of updes_solve_workspace); updes_solve_factored then
+ * solves nrhs right-hand sides (the columns of the row-major N x nrhs block Q,
+ * leading dimension ldq) against those factors, writing coeffs (n x nrhs, ldc)
+ * and vals (N x nrhs, ldv, may be NULL), each refined in FP64 like updes_solve
+ * (an FP64 refactorisation replaces the factors if refinement stalls).
+ * updes_solve is updes_factor followed by one updes_solve_factored column.
+ * The reference rebuilds and refactors on every call (time stepping in
+ * demos/Advection/00_advection_with_rbf.py:83-93, two solves per epoch in
+ * demos/Laplace/03_laplace_with_adjoint.py:88-143).
+ */
+UPDES_API int updes_factor(const updes_problem* p, const updes_solve_opts* opts, updes_solve_info* info,
+                           void* workspace, size_t workspace_bytes, void* stream);
+UPDES_API int updes_solve_factored(const updes_problem* p, int32_t nrhs, const double* Q, int64_t ldq,
+                                   double* coeffs, int64_t ldc, double* vals, int64_t ldv,
+                                   const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                                   size_t workspace_bytes, void* stream);
+
+/* ---- adjoint (reverse mode through the solve) ------------------------------
+ * The reference differentiates pde_solver with jax.grad through inv, the GEMM
+ * and the lineax QR (demos/Laplace/10_laplace_with_diff_phys.py:89-104) or runs
+ * a second full solve for a hand-written adjoint
+ * (demos/Laplace/03_laplace_with_adjoint.py:98-108).  Here the adjoint reuses
+ * the forward factors:  with K c = [q; 0] and vals = [Phi P] c,
+ *   g       = dJ/dc + [Phi P]^T dJ/dvals               (updes_eval_values_t)
+ *   lambda  = K^-T g                                   (updes_solve_transpose)
+ *   dJ/dq   = lambda[0:N]
+ *   dJ/dW_i = -lambda_i (D c)_i per interior row        (updes_coeff_grad)
+ * where W_i are the operator weights of row i and D the five primitives.
+ */
+
+/* out (n) = [Phi P]^T g for g (N): Phi g (Phi symmetric) then P^T g. */
+UPDES_API int updes_eval_values_t(const updes_problem* p, const double* g, double* out, void* stream);
+
+/*
+ * lambda (n) = K^-T g (n) with the factors that the last updes_solve on this
+ * workspace left there (FP64 GMRES refinement on K^T, same stopping test).
+ * Returns UPDES_ERR_INVALID if the workspace holds no factorisation of an
+ * n x n system.
+ */
+UPDES_API int updes_solve_transpose(const updes_problem* p, const double* g, double* lambda,
+                                    const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                                    size_t workspace_bytes, void* stream);
+
+/* dW (Ni x 5) = -lambda_i * sum_j D_k(x_i, x_j) c_j (monomial columns included), entries regenerated
+ * on the fly (no matrix is stored). */
+UPDES_API int updes_coeff_grad(const updes_problem* p, const double* coeffs, const double* lambda, double* dW,
+                               void* stream);
+
 /* ---- instrumentation ------------------------------------------------------ */
 
 /* Kernel classes of updes_stats: 0 trailing update, 1 panel, 2 TRSM, 3 triangular

@@ -197,3 +197,107 @@ def test_residual_kernel():
         _lib.check(lib.updes_residual(n, Ad.data_ptr(), ld, xd.data_ptr(), bd.data_ptr(), r.data_ptr(), trans, s), "r")
         want = b - (A.T if trans else A) @ x
         assert rel(r.cpu().numpy(), want) < 1e-13
+
+
+def _factor_both(n, seed):
+    import torch
+    lib = _lib.load()
+    A = _rand_system(n, seed)
+    ld = int(lib.updes_matrix_ld(n, 8))
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {}
+    for precision in (0, 1):
+        Ad = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+        Ad[:, :n] = torch.as_tensor(A)
+        F = torch.zeros((n, ld), dtype=torch.float32, device="cuda") if precision else Ad
+        piv = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+        nb = ctypes.c_size_t()
+        _lib.check(lib.updes_lu_workspace(n, precision, ctypes.byref(nb)), "ws")
+        ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+        info = ctypes.c_int32(-1)
+        _lib.check(lib.updes_lu_factor(n, Ad.data_ptr(), ld, precision, F.data_ptr() if precision else None,
+                                       ld if precision else 0, piv.data_ptr(), ws.data_ptr(), ws.numel(),
+                                       ctypes.byref(info), s), "factor")
+        assert info.value == 0
+        out[precision] = (F[:, :n].double().cpu().numpy(), piv[:n].cpu().numpy())
+    return out
+
+
+@pytest.mark.parametrize("n", [70, 300, 700])
+def test_mixed_factorisation_backward_error(n):
+    """P A = L U holds to FP32-rounding level, |P A - L U| <= 2^-22 (|L| |U|) entrywise, for the FP32
+    factors of the mixed LU (tensor-core digit-product updates in a double-float trailing matrix)."""
+    out = _factor_both(n, 100 + n)
+    A = _rand_system(n, 100 + n)
+    for precision, tol in ((1, 2.0 ** -22), (0, 2.0 ** -48)):
+        F, piv = out[precision]
+        perm = np.arange(n)
+        for i, p in enumerate(piv):
+            perm[[i, p]] = perm[[p, i]]
+        L = np.tril(F, -1) + np.eye(n)
+        U = np.triu(F)
+        R = np.abs(A[perm] - L @ U)
+        bound = tol * (np.abs(L) @ np.abs(U)) + 1e-300
+        assert np.all(R <= bound), (precision, (R / bound).max())
+
+
+def test_mixed_refinement_iterations_on_ill_conditioned_system():
+    """The Poisson r^3 / degree-2 system at N = 3,600 (kappa(K) ~ 1e10): an FP32-accumulated LU
+    (LAPACK sgetrf) needs ~100 GMRES iterations here, an LU whose trailing updates are accurate needs
+    a handful.  The mixed path must stay in the second class, without falling back to FP64."""
+    import updes_gb300 as U
+    facets = {"South": "d", "West": "d", "North": "d", "East": "d"}
+    cl = U.SquareCloud(Nx=60, Ny=60, facet_types=facets, jitter=(0.2, 0))
+    ustar = lambda c: np.sin(np.pi * c[0]) * np.sin(np.pi * c[1])
+    op = lambda x, center, rbf, monomial, fields: U.nodal_laplacian(x, center, rbf, monomial)
+    rhs = lambda x, centers, rbf, fields: -2 * np.pi ** 2 * np.sin(np.pi * x[0]) * np.sin(np.pi * x[1])
+    s32 = U.pde_solver(op, rhs, cl, {f: ustar for f in facets}, U.polyharmonic, 2,
+                       options=U.SolverOptions(precision="fp32"))
+    info = dict(U.LAST_INFO)
+    s64 = U.pde_solver(op, rhs, cl, {f: ustar for f in facets}, U.polyharmonic, 2,
+                       options=U.SolverOptions(precision="fp64"))
+    assert info["fell_back"] == 0 and info["converged"] == 1, info
+    assert info["iters"] <= 12, info
+    assert rel(s32.vals, s64.vals) < 1e-8
+
+
+def test_factor_once_solve_many():
+    """updes_factor + updes_solve_factored on 3 right-hand sides equals 3 fresh updes_solve calls, and
+    pde_solver reuses its factors when only the boundary values change."""
+    import torch
+
+    import updes_gb300 as U
+    from gpu_helpers import device_problem
+    lib = _lib.load()
+    g = load("readme_laplace_30x20")
+    case = case_of(g)
+    cl, dp, q = device_problem(case)
+    rng = np.random.default_rng(3)
+    Q = np.stack([q, q + rng.standard_normal(q.shape) * 0.1, 2 * q], axis=1)  # N x 3
+    opts = U.SolverOptions(precision="fp32")
+    co = opts.c_opts()
+    nb = ctypes.c_size_t()
+    _lib.check(lib.updes_solve_workspace(ctypes.byref(dp.c), ctypes.byref(co), ctypes.byref(nb)), "ws")
+    ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    info = _lib.SolveInfo()
+    _lib.check(lib.updes_factor(ctypes.byref(dp.c), ctypes.byref(co), ctypes.byref(info), ws.data_ptr(), ws.numel(),
+                                dp.stream()), "factor")
+    Qd = torch.as_tensor(Q, device="cuda").contiguous()
+    Cd = torch.empty((dp.n, 3), dtype=torch.float64, device="cuda")
+    Vd = torch.empty((dp.N, 3), dtype=torch.float64, device="cuda")
+    _lib.check(lib.updes_solve_factored(ctypes.byref(dp.c), 3, Qd.data_ptr(), 3, Cd.data_ptr(), 3, Vd.data_ptr(), 3,
+                                        ctypes.byref(co), ctypes.byref(info), ws.data_ptr(), ws.numel(), dp.stream()),
+               "solve_factored")
+    for j in range(3):
+        c1, v1, _ = U.operators.solve_device(dp, Q[:, j], U.SolverOptions(precision="fp32", reuse_factorization=False))
+        assert rel(Vd[:, j].cpu().numpy(), v1.cpu().numpy()) < 1e-11
+        assert rel(Cd[:, j].cpu().numpy(), c1.cpu().numpy()) < 1e-8
+    # transparent reuse inside pde_solver
+    from gpu_helpers import solve_case
+    U.operators.free_factorizations()
+    _, s1 = solve_case(case, "fp32")
+    assert not U.LAST_INFO["reused_factors"]
+    _, s2 = solve_case(case, "fp32")
+    assert U.LAST_INFO["reused_factors"]
+    assert rel(s2.vals, s1.vals) < 1e-12
+    assert rel(s1.vals, g["vals"]) < 1e-8

@@ -95,6 +95,14 @@ SIGNATURES = {
                                              ctypes.POINTER(_sz)]),
     "updes_solve": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp, ctypes.POINTER(SolveOpts),
                                    ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),
+    "updes_factor": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo),
+                                    _vp, _sz, _vp]),
+    "updes_solve_factored": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _i64, _vp, _i64, _vp, _i64,
+                                            ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),
+    "updes_eval_values_t": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp]),
+    "updes_solve_transpose": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, ctypes.POINTER(SolveOpts),
+                                             ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),
+    "updes_coeff_grad": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp, _vp]),
     "updes_stats_reset": (None, [_i32]),
     "updes_stats_read": (None, [ctypes.POINTER(Stats)]),
 }

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(updes_problem p, int n, d
 constexpr int kEvalRows = 16;     // rows per CTA (2 per warp)
 constexpr int kEvalChunk = 512;   // columns staged per pass
 
-template <int KIND>
+template <int KIND, bool POLY = true>
 __global__ void __launch_bounds__(256) eval_values_kernel(updes_problem p, const double* __restrict__ coeffs,
                                                           double* __restrict__ vals) {
   __shared__ double sx[kEvalChunk], sy[kEvalChunk], sc[kEvalChunk];
@@ -216,7 +216,8 @@ __global__ void __launch_bounds__(256) eval_values_kernel(updes_problem p, const
     const int r = r0 + lane;
     if (r < p.N) {
       double s = acc[lane];
-      for (int k = 0; k < p.M; ++k) s += monomial_terms(k, xi[lane], yi[lane]).m * coeffs[p.N + k];
+      if (POLY)
+        for (int k = 0; k < p.M; ++k) s += monomial_terms(k, xi[lane], yi[lane]).m * coeffs[p.N + k];
       vals[r] = s;
     }
   }
@@ -284,6 +285,90 @@ __global__ void __launch_bounds__(256) eval_field_kernel(int m, const double* __
       if (what == 1) { out[2 * r] = v0; out[2 * r + 1] = v1; }
       else out[r] = v0;
     }
+  }
+}
+
+// dW[i][k] = -lambda_i * sum_j D_k(x_i, x_j) c_j (+ monomial columns) for interior rows i, where D_k is the
+// k-th operator primitive (value, d/dx, d/dy, d2/dx2, d2/dy2) and j != i unless self_term: the derivative
+// of lambda^T K c with respect to the operator weights of row i, the entries regenerated on the fly.
+template <int KIND>
+__global__ void __launch_bounds__(256) coeff_grad_kernel(updes_problem p, const double* __restrict__ coeffs,
+                                                         const double* __restrict__ lambda,
+                                                         double* __restrict__ dW) {
+  __shared__ double sx[kEvalChunk], sy[kEvalChunk], sc[kEvalChunk];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int r0 = blockIdx.x * kEvalRows + warp * 2;
+  double xi[2], yi[2], acc[2][5] = {};
+  for (int u = 0; u < 2; ++u) {
+    const int r = min(r0 + u, max(p.Ni - 1, 0));
+    xi[u] = p.nodes[2 * r];
+    yi[u] = p.nodes[2 * r + 1];
+  }
+  for (int base = 0; base < p.N; base += kEvalChunk) {
+    __syncthreads();
+    for (int t = tid; t < kEvalChunk; t += blockDim.x) {
+      const int c = base + t;
+      if (c < p.N) { sx[t] = p.nodes[2 * c]; sy[t] = p.nodes[2 * c + 1]; sc[t] = coeffs[c]; }
+      else { sx[t] = sy[t] = sc[t] = 0.0; }
+    }
+    __syncthreads();
+    const int lim = min(kEvalChunk, p.N - base);
+    for (int t = lane; t < lim; t += 32) {
+      const int c = base + t;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (c == r0 + u && !p.self_term) continue;
+        const double dx = xi[u] - sx[t], dy = yi[u] - sy[t];
+        const double r2 = dx * dx + dy * dy;
+        const double cj = sc[t];
+        if (r2 == 0.0) { acc[u][0] += rbf_phi0<KIND>() * cj; continue; }
+        const RbfG g = rbf_g<KIND>(r2, p.rbf_param, ip);
+        acc[u][0] += g.phi * cj;
+        acc[u][1] += g.g1 * dx * cj;
+        acc[u][2] += g.g1 * dy * cj;
+        acc[u][3] += (g.g1 + g.g2 * dx * dx) * cj;
+        acc[u][4] += (g.g1 + g.g2 * dy * dy) * cj;
+      }
+    }
+  }
+  for (int u = 0; u < 2; ++u)
+    for (int k = 0; k < 5; ++k)
+      for (int o = 16; o > 0; o >>= 1) acc[u][k] += __shfl_xor_sync(0xffffffffu, acc[u][k], o);
+  if (lane < 2) {
+    const int r = r0 + lane;
+    if (r < p.Ni) {
+      double v[5];
+      for (int k = 0; k < 5; ++k) v[k] = acc[lane][k];
+      for (int m = 0; m < p.M; ++m) {
+        const MonoT mt = monomial_terms(m, xi[lane], yi[lane]);
+        const double gm = coeffs[p.N + m];
+        v[0] += mt.m * gm; v[1] += mt.mx * gm; v[2] += mt.my * gm; v[3] += mt.mxx * gm; v[4] += mt.myy * gm;
+      }
+      const double l = lambda[r];
+      for (int k = 0; k < 5; ++k) dW[5 * r + k] = -l * v[k];
+    }
+  }
+}
+
+// out[N + k] = sum_i m_k(x_i) g_i  (the P^T part of A^T g)
+__global__ void pt_matvec_kernel(updes_problem p, const double* __restrict__ g, double* __restrict__ out) {
+  __shared__ double red[15][32];
+  double acc[15] = {};
+  for (int i = threadIdx.x; i < p.N; i += blockDim.x) {
+    const double gi = g[i];
+    for (int k = 0; k < p.M; ++k) acc[k] += monomial_terms(k, p.nodes[2 * i], p.nodes[2 * i + 1]).m * gi;
+  }
+  for (int k = 0; k < p.M; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < p.M) {
+    double v = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+    out[p.N + threadIdx.x] = v;
   }
 }
 
@@ -366,6 +451,45 @@ extern "C" int updes_eval_field(int32_t m, const double* points, int32_t N, cons
     case UPDES_RBF_INVERSE_MULTIQUADRIC: eval_field_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
     default: eval_field_kernel<UPDES_RBF_THIN_PLATE><<<grid, 256, 0, s>>>(m, points, N, centers, M, rbf_param, coeffs, what, out); break;
   }
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+extern "C" int updes_coeff_grad(const updes_problem* p, const double* coeffs, const double* lambda, double* dW,
+                                void* stream) {
+  int st = check_problem(p);
+  if (st) return st;
+  if (!coeffs || !lambda || !dW) return UPDES_ERR_INVALID;
+  if (p->Ni == 0) return UPDES_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const unsigned grid = unsigned(ceil_div(p->Ni, kEvalRows));
+  switch (p->rbf) {
+    case UPDES_RBF_POLYHARMONIC: coeff_grad_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, coeffs, lambda, dW); break;
+    case UPDES_RBF_GAUSSIAN: coeff_grad_kernel<UPDES_RBF_GAUSSIAN><<<grid, 256, 0, s>>>(*p, coeffs, lambda, dW); break;
+    case UPDES_RBF_MULTIQUADRIC: coeff_grad_kernel<UPDES_RBF_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, coeffs, lambda, dW); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC: coeff_grad_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, coeffs, lambda, dW); break;
+    default: coeff_grad_kernel<UPDES_RBF_THIN_PLATE><<<grid, 256, 0, s>>>(*p, coeffs, lambda, dW); break;
+  }
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+extern "C" int updes_eval_values_t(const updes_problem* p, const double* g, double* out, void* stream) {
+  int st = check_problem(p);
+  if (st) return st;
+  if (!g || !out) return UPDES_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const unsigned grid = unsigned(ceil_div(p->N, kEvalRows));
+  // Phi is symmetric (radial kernel, same zero diagonal), so Phi^T g = Phi g
+  switch (p->rbf) {
+    case UPDES_RBF_POLYHARMONIC: eval_values_kernel<UPDES_RBF_POLYHARMONIC, false><<<grid, 256, 0, s>>>(*p, g, out); break;
+    case UPDES_RBF_GAUSSIAN: eval_values_kernel<UPDES_RBF_GAUSSIAN, false><<<grid, 256, 0, s>>>(*p, g, out); break;
+    case UPDES_RBF_MULTIQUADRIC: eval_values_kernel<UPDES_RBF_MULTIQUADRIC, false><<<grid, 256, 0, s>>>(*p, g, out); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC: eval_values_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC, false><<<grid, 256, 0, s>>>(*p, g, out); break;
+    default: eval_values_kernel<UPDES_RBF_THIN_PLATE, false><<<grid, 256, 0, s>>>(*p, g, out); break;
+  }
+  UPDES_LAUNCH_CHECK();
+  pt_matvec_kernel<<<1, 1024, 0, s>>>(*p, g, out);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }

@@ -1,9 +1,365 @@
-// Tensor-core trailing update of the mixed-precision LU (not yet enabled:
-// the SIMT FP64-accumulating update in lu.cu runs instead).
-#include "gemm_tc.cuh"
+// Tensor-core trailing update of the mixed-precision LU (sm_103a, tcgen05).
+//
+//   C  <-  C - A * B        C: FP32 hi/lo pairs ("double-float", ~48 bits)
+//                           A: m x K FP32 (L factor block), B: K x nc FP32 (U factor block)
+//
+// Every FP32 operand is written as D bf16 integer digits (D = UPDES_OZAKI_DIGITS,
+// 3 by default) under a power-of-two scale shared by a row of A (a column of
+// B) over each 64-wide k-block:
+//   a = 2^(eA-8) * (d1 + 2^-9 d2 + 2^-18 d3 + ...),   |d_i| <= 256 (exact in bf16),
+// exact for entries within 2^(9D-25) of the row maximum and otherwise cut at
+// 2^-(9D-1) of it.  Digit products are <= 2^16, a 64-term sum is <= 2^22 and a
+// group of at most D products of equal weight 2^-9g stays <= 2^24, so each of
+// the 2D-1 FP32 TMEM accumulators holds an exact integer: the tensor cores add
+// no rounding (FP32-accumulated updates lose the Schur complements of these
+// ill-conditioned matrices).  The epilogue folds the groups into a
+// double-float value and subtracts it from C with error-free transformations
+// (FP32 ALU only; FP64 throughput is low on GB300).
+// Each CTA owns a 128 x 64 tile of C; one thread issues tcgen05.mma
+// (kind::f16, bf16 operands from 128B-swizzled K-major shared memory, FP32
+// accumulators in tensor memory); every wait is bounded.
+#include <cuda_bf16.h>
 
-bool gemm_tc_enabled() { return false; }
-size_t gemm_tc_workspace_bytes(int n) { (void)n; return 0; }
-int gemm_tc_update(void*, int, int, int, double*, int64_t, const void*, int64_t, cudaStream_t) {
-  return UPDES_ERR_UNSUPPORTED;
+#include "gemm_tc.cuh"
+#include "stats.cuh"
+
+#ifndef UPDES_OZAKI_DIGITS
+#define UPDES_OZAKI_DIGITS 3
+#endif
+
+namespace {
+
+constexpr int TM = 128, TN = 64, TK = 64;
+constexpr int kThreads = 256;
+constexpr uint32_t kTmemCols = 512;  // kGroups x 64 columns, rounded to a power of two
+constexpr int kDigits = UPDES_OZAKI_DIGITS, kGroups = 2 * kDigits - 1;
+static_assert(kGroups * TN <= int(kTmemCols), "accumulators must fit in tensor memory");
+constexpr int kATile = TM * TK * 2;  // 16 KB per digit plane
+constexpr int kBTile = TN * TK * 2;  //  8 KB per digit plane
+constexpr int kSmemOperands = kDigits * (kATile + kBTile);
+// 120 KB: more than half of an SM's shared memory, so one CTA per SM (it owns 512 TMEM columns)
+constexpr int kSmemBytes = 120 * 1024;
+static_assert(kSmemOperands + 1024 + 1024 + 64 <= kSmemBytes, "shared memory layout");
+
+// instruction descriptor: D = F32, A = B = BF16, both K-major, N = 64, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128B swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = uint64_t((saddr & 0x3FFFFu) >> 4);
+  d |= uint64_t(1) << 16;             // leading byte offset (unused with 128B swizzle, K-major)
+  d |= uint64_t(1024 >> 4) << 32;     // stride byte offset
+  d |= uint64_t(1) << 46;             // descriptor version
+  d |= uint64_t(2) << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// byte offset of element (row, k) of a K-major, 128B-swizzled bf16 tile (64 k per row)
+__device__ __forceinline__ uint32_t sw128(int row, int k) {
+  return uint32_t((row >> 3) * 1024 + (row & 7) * 128 + ((((k >> 3) ^ row) & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ float pow2f(int e) {  // 2^e for e in [-126, 127]
+  return __int_as_float((e + 127) << 23);
+}
+
+// exponent e with max < 2^e (frexp convention), clamped so that scalings stay in range
+__device__ __forceinline__ int exp_of(float mx) {
+  const int E = (__float_as_int(mx) >> 23) & 0xFF;
+  if (E == 0) return -100;  // zero or subnormal: digits round to zero
+  return max(E - 126, -100);
+}
+
+// a * scale = d[0] + 2^-9 d[1] + 2^-18 d[2] + ... (+ a remainder below the last digit), |d[i]| <= 256
+__device__ __forceinline__ void digits(float a, float scale, float (&d)[kDigits]) {
+  float r = __fmul_rn(a, scale);  // exact: power-of-two scaling, |r| <= 256
+#pragma unroll
+  for (int i = 0; i < kDigits; ++i) {
+    d[i] = rintf(r);
+    r = __fmul_rn(__fsub_rn(r, d[i]), 512.f);  // exact: |r - d| <= 1/2
+  }
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
+  for (long long it = 0; it < kSpinLimit; ++it) {
+    if (mbar_try_wait(bar, phase)) return true;
+    __nanosleep(32);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__global__ void __launch_bounds__(kThreads, 1)
+    ozaki_update_kernel(float* __restrict__ Chi, float* __restrict__ Clo, int64_t ldc, const float* __restrict__ A,
+                        int64_t lda, const float* __restrict__ B, int64_t ldb, int m, int nc, int K,
+                        DeviceStatus* st) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;                              // 3 x 16 KB
+  uint8_t* sB = smem + kDigits * kATile;           // 3 x 8 KB
+  float* sSA = reinterpret_cast<float*>(smem + kSmemOperands);  // 128 row scales 2^(eA-8)
+  float* sSB = sSA + TM;                                        // 64 column scales 2^(eB-8)
+  float* sBmax = sSB + TN;                                      // 4 x 64 partial column maxima
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_fail;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int r0 = blockIdx.y * TM, c0 = blockIdx.x * TN;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_fail = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  uint32_t phase = 0, failed_phase = 0;
+
+  for (int kb = 0; kb < K; kb += TK) {
+    // ---- A: 128 rows x 64 k, row max over the block, 3 digit planes ----
+#pragma unroll 1
+    for (int it = 0; it < 4; ++it) {
+      const int chunk = tid + it * kThreads;  // 1024 chunks of 8 k-values
+      const int row = chunk >> 3, kc = chunk & 7;
+      float v[8];
+      const int gr = r0 + row;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = kb + kc * 8 + u;
+        v[u] = (gr < m && k < K) ? A[int64_t(gr) * lda + k] : 0.f;
+      }
+      float mx = 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(v[u]));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 4));
+      const int e = exp_of(mx);
+      if (kc == 0) sSA[row] = pow2f(e - 8);
+      const float scale = pow2f(8 - e);
+      __align__(16) __nv_bfloat16 d[kDigits][8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        float dd[kDigits];
+        digits(v[u], scale, dd);
+#pragma unroll
+        for (int p = 0; p < kDigits; ++p) d[p][u] = __float2bfloat16_rn(dd[p]);
+      }
+      const uint32_t off = sw128(row, kc * 8);
+#pragma unroll
+      for (int p = 0; p < kDigits; ++p)
+        *reinterpret_cast<uint4*>(sA + p * kATile + off) = *reinterpret_cast<uint4*>(d[p]);
+    }
+    // ---- B: 64 k x 64 columns, column max, stored transposed (row = column j, K-major) ----
+    {
+      const int j = tid & 63, kq = tid >> 6;  // 4 quarters of 16 k
+      const int gc = c0 + j;
+      float v[16];
+      float mx = 0.f;
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int k = kb + kq * 16 + u;
+        v[u] = (gc < nc && k < K) ? B[int64_t(k) * ldb + gc] : 0.f;
+        mx = fmaxf(mx, fabsf(v[u]));
+      }
+      sBmax[kq * TN + j] = mx;
+      __syncthreads();
+      mx = fmaxf(fmaxf(sBmax[j], sBmax[TN + j]), fmaxf(sBmax[2 * TN + j], sBmax[3 * TN + j]));
+      const int e = exp_of(mx);
+      if (kq == 0) sSB[j] = pow2f(e - 8);
+      const float scale = pow2f(8 - e);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        __align__(16) __nv_bfloat16 d[kDigits][8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          float dd[kDigits];
+          digits(v[h * 8 + u], scale, dd);
+#pragma unroll
+          for (int p = 0; p < kDigits; ++p) d[p][u] = __float2bfloat16_rn(dd[p]);
+        }
+        const uint32_t off = sw128(j, kq * 16 + h * 8);
+#pragma unroll
+        for (int p = 0; p < kDigits; ++p)
+          *reinterpret_cast<uint4*>(sB + p * kBTile + off) = *reinterpret_cast<uint4*>(d[p]);
+      }
+    }
+    // generic-proxy smem writes -> visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    // ---- kDigits^2 digit products x 4 k-steps into kGroups accumulators ----
+    if (tid == 0) {
+      tc_fence_after();
+      bool started[kGroups] = {};
+#pragma unroll 1
+      for (int a = 0; a < kDigits; ++a) {
+#pragma unroll 1
+        for (int b = 0; b < kDigits; ++b) {
+          const int g = a + b;
+          const uint32_t d_tmem = tmem + uint32_t(g * TN);
+          const uint32_t abase = smem_u32(sA + a * kATile), bbase = smem_u32(sB + b * kBTile);
+#pragma unroll
+          for (int kk = 0; kk < TK / 16; ++kk) {
+            mma_bf16(d_tmem, make_desc(abase + kk * 32), make_desc(bbase + kk * 32), started[g] ? 1u : 0u);
+            started[g] = true;
+          }
+        }
+      }
+      mma_commit(&mbar);
+    }
+    __syncwarp();
+    // ---- wait for the accumulators ----
+    if (!mbar_wait_bounded(&mbar, phase)) {
+      s_fail = 1;
+      failed_phase = phase;
+    }
+    phase ^= 1u;
+    tc_fence_after();
+    __syncthreads();
+    if (s_fail) break;
+    // ---- epilogue: warps w and w+4 share TMEM lanes 32(w%4).., columns split in halves ----
+    {
+      const int row = (warp & 3) * 32 + lane;
+      const int gr = r0 + row;
+      const uint32_t lane_base = uint32_t((warp & 3) * 32) << 16;
+      const float sa = sSA[row];
+#pragma unroll 1
+      for (int ch = 0; ch < 2; ++ch) {
+        const int col = (warp >> 2) * 32 + ch * 16;
+        float acc[kGroups][16];
+#pragma unroll
+        for (int g = 0; g < kGroups; ++g) tmem_ld16(tmem + lane_base + uint32_t(g * TN + col), acc[g]);
+        tmem_wait_ld();
+        if (gr < m) {
+          float* ph = Chi + int64_t(gr) * ldc;
+          float* pl = Clo + int64_t(gr) * ldc;
+#pragma unroll 4
+          for (int u = 0; u < 16; ++u) {
+            const int gc = c0 + col + u;
+            if (gc >= nc) break;
+            // s = sum_g acc_g 2^(-9g) as a double-float (acc_g are exact integers)
+            float h, l, e;
+            two_sum(acc[0][u], __fmul_rn(acc[1][u], 1.953125e-3f), h, l);
+            two_sum(h, __fmul_rn(acc[2][u], 3.814697265625e-06f), h, e);
+            l = __fadd_rn(l, e);
+            float w = 3.814697265625e-06f;
+#pragma unroll
+            for (int g = 3; g < kGroups; ++g) {
+              w = __fmul_rn(w, 1.953125e-3f);
+              l = __fadd_rn(l, __fmul_rn(acc[g][u], w));
+            }
+            fast_two_sum(h, l, h, l);
+            const float sc = __fmul_rn(sa, sSB[col + u]);
+            h = __fmul_rn(h, sc);
+            l = __fmul_rn(l, sc);
+            // C -= (h, l)
+            float s, t;
+            two_sum(ph[gc], -h, s, t);
+            t = __fadd_rn(t, __fsub_rn(pl[gc], l));
+            fast_two_sum(s, t, s, t);
+            ph[gc] = s;
+            pl[gc] = t;
+          }
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (s_fail && tid == 0) {
+    status_error(st, UPDES_ERR_TIMEOUT);
+    atomicCAS(&st->timeout_tag, 0, 40);
+    // give in-flight MMAs a bounded chance to finish before the tensor memory is released
+    mbar_wait_bounded(&mbar, failed_phase);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+}  // namespace
+
+
+int ozaki_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
+                 int m, int nc, int K, DeviceStatus* st, cudaStream_t s) {
+  if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
+  static bool attr = false;
+  if (!attr) {
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(ozaki_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    attr = true;
+  }
+  dim3 grid(unsigned(ceil_div(nc, TN)), unsigned(ceil_div(m, TM)));
+  StatScope sc(kStatGemm, s, 2.0 * m * double(nc) * K, double(m) * nc * 16.0 + (double(m) + nc) * K * 4.0);
+  ozaki_update_kernel<<<grid, kThreads, kSmemBytes, s>>>(Chi, Clo, ldc, A, lda, B, ldb, m, nc, K, st);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
 }

@@ -3,12 +3,7 @@
 
 #include "common.cuh"
 
-struct GemmTcCtx {
-  void* ws;
-  size_t ws_bytes;
-};
 
-bool gemm_tc_enabled();
-size_t gemm_tc_workspace_bytes(int n);
-int gemm_tc_update(void* ctx, int n, int k, int nb, double* W, int64_t ldw, const void* F, int64_t ldf,
-                   cudaStream_t s);
+// C (double-float planes hi/lo, ldc) -= A (m x K FP32, lda) * B (K x nc FP32, ldb), products exact.
+int ozaki_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
+                 int m, int nc, int K, DeviceStatus* st, cudaStream_t s);

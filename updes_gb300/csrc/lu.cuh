@@ -20,3 +20,9 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
 // mode: 0 = L, 1 = U, 2 = U^T, 3 = L^T (x overwritten in place); sync_ws: ceil(n/64)+1 ints.
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s);
+
+// Mixed LU on a double-float working matrix (Whi, Wlo FP32 planes): factors in FP32 (overwriting Whi),
+// every trailing update formed exactly on the tensor cores and accumulated in double-float.
+size_t lu_df_workspace_bytes(int n);
+int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* ws, size_t ws_bytes, DeviceStatus* st,
+                 cudaStream_t s);

@@ -135,20 +135,30 @@ __global__ void bwd_partial_kernel(const double* __restrict__ r, const double* _
 __global__ void __launch_bounds__(256) gemv_t_kernel(const double* __restrict__ K, int64_t ld, int n,
                                                      const double* __restrict__ x, const double* __restrict__ b,
                                                      const double* __restrict__ dr, const double* __restrict__ dc,
-                                                     double bsign, double ksign, double* __restrict__ out) {
-  __shared__ double part[8][33];
+                                                     double bsign, double ksign, double* __restrict__ out,
+                                                     double* __restrict__ absout = nullptr) {
+  __shared__ double part[8][33], apart[8][33];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j = blockIdx.x * 32 + lane;
-  double s = 0.0;
+  double s = 0.0, a = 0.0;
   if (j < n)
-    for (int i = w; i < n; i += 8) s = fma(K[int64_t(i) * ld + j], dr ? dr[i] * x[i] : x[i], s);
+    for (int i = w; i < n; i += 8) {
+      const double t = K[int64_t(i) * ld + j] * (dr ? dr[i] * x[i] : x[i]);
+      s += t;
+      a += fabs(t);
+    }
   part[w][lane] = s;
+  apart[w][lane] = a;
   __syncthreads();
   if (w == 0 && j < n) {
-    double t = 0.0;
-    for (int q = 0; q < 8; ++q) t += part[q][lane];
+    double t = 0.0, ta = 0.0;
+    for (int q = 0; q < 8; ++q) {
+      t += part[q][lane];
+      ta += apart[q][lane];
+    }
     double v = ksign * t + (b ? bsign * b[j] : 0.0);
     out[j] = dc ? dc[j] * v : v;
+    if (absout) absout[j] = (dc ? dc[j] : 1.0) * (ta + (b ? fabs(b[j]) : 0.0));
   }
 }
 
@@ -276,20 +286,19 @@ struct LuWs {
   size_t panel_bytes;
   int* sync;
   double* tmp;
-  void* gemm_ws;
-  size_t gemm_bytes;
+  float* lo;  // lo plane of the double-float working matrix (FP32 precision, when owned here)
 };
 
-size_t lu_ws_layout(int n, int precision, char* base, LuWs* out) {
+// lo_plane: reserve the n x ld FP32 lo plane (updes_lu_factor); updes_solve brings its own.
+size_t lu_ws_layout(int n, int precision, char* base, LuWs* out, bool lo_plane = true) {
   Carve c{base};
   LuWs w;
   w.st = c.take<DeviceStatus>(1);
-  w.panel_bytes = lu_panel_workspace_bytes(kLuNb);
+  w.panel_bytes = precision == UPDES_PREC_FP32 ? lu_df_workspace_bytes(n) : lu_panel_workspace_bytes(kLuNb);
   w.panel = c.take<char>(w.panel_bytes);
   w.sync = c.take<int>(ceil_div(n, 64) + 2);
   w.tmp = c.take<double>(n);
-  w.gemm_bytes = (precision == UPDES_PREC_FP32) ? gemm_tc_workspace_bytes(n) : 0;
-  w.gemm_ws = c.take<char>(w.gemm_bytes);
+  w.lo = (precision == UPDES_PREC_FP32 && lo_plane) ? c.take<float>(size_t(n) * updes_matrix_ld(n, 4)) : nullptr;
   if (out) *out = w;
   return c.off + 256;
 }
@@ -300,11 +309,53 @@ int read_status(DeviceStatus* st, cudaStream_t s, DeviceStatus* host) {
   return UPDES_OK;
 }
 
+// hi = float(v), lo = float(v - hi) with v = dr_i K_ij dc_j (scalings exact; dr, dc may be null)
+__global__ void split_df_kernel(const double* __restrict__ K, int64_t ldk, float* __restrict__ hi,
+                                float* __restrict__ lo, int64_t ld, int n, const double* __restrict__ dr,
+                                const double* __restrict__ dc) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t i = e / ld, j = e % ld;
+  if (i >= n) return;
+  double v = 0.0;
+  if (j < n) {
+    v = K[i * ldk + j];
+    if (dr) v *= dr[i];
+    if (dc) v *= dc[j];
+  }
+  const float h = float(v);
+  hi[i * ld + j] = h;
+  lo[i * ld + j] = float(v - double(h));
+}
+
+int perm_core(int n, int32_t* piv, cudaStream_t s) {
+  if (n > kMaxPermN) return UPDES_ERR_UNSUPPORTED;
+  UPDES_CUDA_TRY(cudaFuncSetAttribute(perm_from_piv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(n * sizeof(int32_t))));
+  perm_from_piv_kernel<<<1, 1024, n * sizeof(int32_t), s>>>(piv, n, piv + n);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+// Mixed LU of a double-float matrix already split into (hi = F, lo).
+int factor_df_core(int n, float* hi, float* lo, int64_t ld, int32_t* piv, const LuWs& w, cudaStream_t s) {
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DeviceStatus), s));
+  int e = lu_factor_df(n, hi, lo, ld, piv, w.panel, w.panel_bytes, w.st, s);
+  if (e) return e;
+  return perm_core(n, piv, s);
+}
+
 int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t ldf, int32_t* piv, const LuWs& w,
                 cudaStream_t s) {
+  if (precision == UPDES_PREC_FP32) {
+    if (!w.lo || !F) return UPDES_ERR_INVALID;
+    split_df_kernel<<<unsigned(ceil_div(int64_t(n) * ldf, 256)), 256, 0, s>>>(A, lda, static_cast<float*>(F), w.lo,
+                                                                              ldf, n, nullptr, nullptr);
+    UPDES_LAUNCH_CHECK();
+    return factor_df_core(n, static_cast<float*>(F), w.lo, ldf, piv, w, s);
+  }
   UPDES_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DeviceStatus), s));
   int e;
-  if (precision == UPDES_PREC_FP64) {
+  {
     double* Fd = F ? static_cast<double*>(F) : A;
     if (Fd != A) {
       UPDES_CUDA_TRY(cudaMemcpy2DAsync(Fd, ldf * 8, A, lda * 8, size_t(n) * 8, n, cudaMemcpyDeviceToDevice, s));
@@ -312,19 +363,9 @@ int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t l
       lda = ldf;
     }
     e = lu_factor_impl<double>(n, A, lda, A, lda, piv, w.panel, w.panel_bytes, w.st, s, nullptr);
-  } else {
-    GemmTcCtx ctx{w.gemm_ws, w.gemm_bytes};
-    LuHooks hooks{&ctx, gemm_tc_update};
-    e = lu_factor_impl<float>(n, A, lda, static_cast<float*>(F), ldf, piv, w.panel, w.panel_bytes, w.st, s,
-                              gemm_tc_enabled() ? &hooks : nullptr);
   }
   if (e) return e;
-  if (n > kMaxPermN) return UPDES_ERR_UNSUPPORTED;
-  UPDES_CUDA_TRY(cudaFuncSetAttribute(perm_from_piv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(n * sizeof(int32_t))));
-  perm_from_piv_kernel<<<1, 1024, n * sizeof(int32_t), s>>>(piv, n, piv + n);
-  UPDES_LAUNCH_CHECK();
-  return UPDES_OK;
+  return perm_core(n, piv, s);
 }
 
 // x (contiguous, n) <- A^-1 x or A^-T x using the permutation in piv[n, 2n)
@@ -371,7 +412,7 @@ extern "C" int updes_lu_factor(int32_t n, double* A, int64_t lda, int32_t precis
                                int32_t* piv, void* workspace, size_t workspace_bytes, int32_t* info, void* stream) {
   if (n <= 0 || !A || lda < n || !piv || !workspace) return UPDES_ERR_INVALID;
   if (precision != UPDES_PREC_FP64 && precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
-  if (precision == UPDES_PREC_FP32 && (!F || ldf < n)) return UPDES_ERR_INVALID;
+  if (precision == UPDES_PREC_FP32 && (!F || ldf < n || ldf != updes_matrix_ld(n, 4))) return UPDES_ERR_INVALID;
   if (precision == UPDES_PREC_FP64 && F && ldf < n) return UPDES_ERR_INVALID;
   if (workspace_bytes < lu_ws_layout(n, precision, nullptr, nullptr)) return UPDES_ERR_WORKSPACE;
   LuWs w;
@@ -434,8 +475,10 @@ namespace {
 struct SolveWs {
   LuWs lu;
   double *K64, *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *partial, *h;
-  float* F32;
+  float* F32;  // hi plane = FP32 factors
+  float* Wlo;
   int32_t* piv;
+  int32_t* state;  // [0] n of the factored system, [1] precision of its factors, [2] 1 when valid
   int64_t ld;
 };
 
@@ -443,14 +486,16 @@ size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* ou
   SolveWs w;
   const int64_t ld = updes_matrix_ld(n, 8);
   Carve c{base};
-  const size_t lub = lu_ws_layout(n, o.precision, nullptr, nullptr);
+  const size_t lub = lu_ws_layout(n, o.precision, nullptr, nullptr, false);
   char* lubase = c.take<char>(lub);
-  if (base) lu_ws_layout(n, o.precision, lubase, &w.lu);
+  if (base) lu_ws_layout(n, o.precision, lubase, &w.lu, false);
   w.ld = ld;
   w.K64 = c.take<double>(size_t(n) * ld);
-  w.W = c.take<double>(size_t(n) * ld);
-  w.F32 = (o.precision == UPDES_PREC_FP32) ? c.take<float>(size_t(n) * ld) : nullptr;
+  w.W = c.take<double>(size_t(n) * ld);  // FP64 working matrix, or the hi and lo FP32 planes
+  w.F32 = reinterpret_cast<float*>(w.W);
+  w.Wlo = w.F32 + size_t(n) * ld;
   w.piv = c.take<int32_t>(2 * size_t(n));
+  w.state = c.take<int32_t>(64);
   w.dr = c.take<double>(n);
   w.dc = c.take<double>(n);
   w.bs = c.take<double>(n);
@@ -527,20 +572,29 @@ struct Timer {
 };
 
 // Ks z = dr .* (K (dc .* z))
-int apply_K(const SolveWs& w, int n, const double* z, double* out, cudaStream_t s) {
+// (trans: Ks^T z = dc .* (K^T (dr .* z)))
+int apply_K(const SolveWs& w, int n, const double* z, double* out, cudaStream_t s, bool trans = false) {
   StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * n);
-  gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, z, nullptr, w.dr, w.dc, 0.0,
-                                                                         1.0, out);
+  if (trans)
+    gemv_t_kernel<<<unsigned(ceil_div(n, 32)), 256, 0, s>>>(w.K64, w.ld, n, z, nullptr, w.dr, w.dc, 0.0, 1.0, out);
+  else
+    gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, z, nullptr, w.dr, w.dc,
+                                                                           0.0, 1.0, out);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }
 
 // out = bs - Ks x; also returns (on the host) the componentwise backward error
 // max_i |out_i| / (|Ks| |x| + |bs|)_i.
-int residual_scaled(const SolveWs& w, int n, const double* x, double* out, double* bwd, cudaStream_t s) {
+int residual_scaled(const SolveWs& w, int n, const double* x, double* out, double* bwd, cudaStream_t s,
+                    bool trans = false) {
   StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * n);
-  gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, x, nullptr, w.dr, w.dc, 0.0,
-                                                                         -1.0, out, w.absr);
+  if (trans)
+    gemv_t_kernel<<<unsigned(ceil_div(n, 32)), 256, 0, s>>>(w.K64, w.ld, n, x, nullptr, w.dr, w.dc, 0.0, -1.0, out,
+                                                             w.absr);
+  else
+    gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, x, nullptr, w.dr, w.dc,
+                                                                           0.0, -1.0, out, w.absr);
   UPDES_LAUNCH_CHECK();
   axpby_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(out, 1.0, w.bs, 1.0, n, nullptr);
   UPDES_LAUNCH_CHECK();
@@ -557,9 +611,9 @@ int residual_scaled(const SolveWs& w, int n, const double* x, double* out, doubl
   return UPDES_OK;
 }
 
-int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s) {
-  if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, 0, w.lu, s);
-  return solve_core<float>(n, w.F32, w.ld, w.piv, x, 0, w.lu, s);
+int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s, bool trans = false) {
+  if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
+  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
 }
 
 [[maybe_unused]] double host_norm(const std::vector<double>& v) {
@@ -570,7 +624,7 @@ int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s) {
 
 // Restarted, right-preconditioned GMRES on Ks x = bs starting from w.x.
 int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, updes_solve_info* info,
-          cudaStream_t s) {
+          cudaStream_t s, bool trans = false) {
   const int m = o.restart;
   const unsigned g = unsigned(ceil_div(n, 256));
   std::vector<double> H(size_t(m + 1) * m), cs(m), sn(m), gv(m + 1), hcol(m + 2);
@@ -582,7 +636,7 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
   double last_beta = INFINITY;
   for (;;) {
     double bwd;
-    if ((e = residual_scaled(w, n, w.x, w.r, &bwd, s))) return e;
+    if ((e = residual_scaled(w, n, w.x, w.r, &bwd, s, trans))) return e;
     double beta2;
     if ((e = multi_dot(w.r, n, 1, w.r, n, w.partial, w.h, &beta2, s))) return e;
     const double beta = std::sqrt(beta2);
@@ -607,8 +661,8 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
     for (; j < m && total < o.max_iters; ++j, ++total) {
       double* vj = w.V + size_t(j) * n;
       UPDES_CUDA_TRY(cudaMemcpyAsync(w.z, vj, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-      if ((e = precond(w, n, precision, w.z, s))) return e;
-      if ((e = apply_K(w, n, w.z, w.wv, s))) return e;
+      if ((e = precond(w, n, precision, w.z, s, trans))) return e;
+      if ((e = apply_K(w, n, w.z, w.wv, s, trans))) return e;
       // CGS2
       std::fill(hcol.begin(), hcol.end(), 0.0);
       for (int pass = 0; pass < 2; ++pass) {
@@ -657,7 +711,7 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
       UPDES_CUDA_TRY(cudaMemcpyAsync(w.h, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s));
       multi_axpy_kernel<<<g, 256, 0, s>>>(w.V, n, j, w.h, 1.0, nullptr, w.z, n);
       UPDES_LAUNCH_CHECK();
-      if ((e = precond(w, n, precision, w.z, s))) return e;
+      if ((e = precond(w, n, precision, w.z, s, trans))) return e;
       axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.z, 1.0, n, nullptr);
       UPDES_LAUNCH_CHECK();
       UPDES_CUDA_TRY(cudaStreamSynchronize(s));
@@ -678,50 +732,74 @@ extern "C" int updes_solve_workspace(const updes_problem* p, const updes_solve_o
   return UPDES_OK;
 }
 
-extern "C" int updes_solve(const updes_problem* p, const double* q, double* coeffs, double* vals,
-                           const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
-                           size_t workspace_bytes, void* stream) {
-  if (updes_check_problem(p) || !q || !coeffs || !workspace) return UPDES_ERR_INVALID;
-  updes_solve_opts o = normalise(opts);
-  if (o.precision != UPDES_PREC_FP64 && o.precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
-  const int n = p->N + p->M;
-  updes_solve_opts olay = o;
-  olay.precision = UPDES_PREC_FP32;
-  if (workspace_bytes < solve_ws_layout(n, olay, nullptr, nullptr)) return UPDES_ERR_WORKSPACE;
-  SolveWs w;
-  solve_ws_layout(n, olay, static_cast<char*>(workspace), &w);
-  updes_solve_info dummy;
-  if (!info) info = &dummy;
-  std::memset(info, 0, sizeof *info);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const unsigned g = unsigned(ceil_div(n, 256));
+namespace {
+
+// Equilibrated copy of K64 -> factors at `precision`; records the factored state in the workspace.
+int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info, cudaStream_t s) {
+  Timer t(s);
   int e;
-  {
-    Timer t(s);
-    if ((e = updes_assemble(p, w.K64, w.ld, nullptr, 0, stream))) return e;
-    row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, w.dr);
+  if (precision == UPDES_PREC_FP64) {
+    scale_copy_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.K64, w.ld, w.W, w.ld, n, w.dr, w.dc);
     UPDES_LAUNCH_CHECK();
-    col_scale_kernel<<<g, 256, 0, s>>>(w.K64, w.ld, n, w.dr, w.dc);
+    e = factor_core(n, w.W, w.ld, precision, nullptr, w.ld, w.piv, w.lu, s);
+  } else {
+    split_df_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.K64, w.ld, w.F32, w.Wlo, w.ld, n,
+                                                                               w.dr, w.dc);
     UPDES_LAUNCH_CHECK();
-    info->t_assemble_ms = t.stop();
+    e = factor_df_core(n, w.F32, w.Wlo, w.ld, w.piv, w.lu, s);
   }
-  int precision = o.precision;
+  if (e) return e;
+  DeviceStatus h;
+  if ((e = read_status(w.lu.st, s, &h))) return e;
+  if (h.error) return h.error;
+  info->lu_info = h.lu_info;
+  info->t_factor_ms += t.stop();
+  const int32_t st3[3] = {n, precision, 1};
+  UPDES_CUDA_TRY(cudaMemcpyAsync(w.state, st3, sizeof st3, cudaMemcpyHostToDevice, s));
+  UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+  return UPDES_OK;
+}
+
+int read_state(const SolveWs& w, int n, int* precision, cudaStream_t s) {
+  int32_t st3[3] = {0, 0, 0};
+  UPDES_CUDA_TRY(cudaMemcpyAsync(st3, w.state, sizeof st3, cudaMemcpyDeviceToHost, s));
+  UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st3[2] != 1 || st3[0] != n) return UPDES_ERR_INVALID;
+  *precision = st3[1];
+  return UPDES_OK;
+}
+
+// Assemble K (FP64) and its power-of-two equilibration.
+int assemble_stage(const updes_problem* p, const SolveWs& w, int n, updes_solve_info* info, cudaStream_t s) {
+  Timer t(s);
+  int e;
+  if ((e = updes_assemble(p, w.K64, w.ld, nullptr, 0, s))) return e;
+  row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, w.dr);
+  UPDES_LAUNCH_CHECK();
+  col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(w.K64, w.ld, n, w.dr, w.dc);
+  UPDES_LAUNCH_CHECK();
+  info->t_assemble_ms += t.stop();
+  return UPDES_OK;
+}
+
+// One right-hand side against the stored factors: refinement, FP64 fallback, coeffs and vals.
+int solve_stage(const updes_problem* p, const SolveWs& w, int n, const double* q, int64_t qstride, double* coeffs,
+                int64_t cstride, double* vals, int64_t vstride, const updes_solve_opts& o, updes_solve_info* info,
+                cudaStream_t s) {
+  const unsigned g = unsigned(ceil_div(n, 256));
+  int precision, e;
+  if ((e = read_state(w, n, &precision, s))) return e;
   for (int attempt = 0; attempt < 2; ++attempt) {
-    {
-      Timer t(s);
-      scale_copy_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.K64, w.ld, w.W, w.ld, n, w.dr, w.dc);
-      UPDES_LAUNCH_CHECK();
-      e = factor_core(n, w.W, w.ld, precision, precision == UPDES_PREC_FP64 ? nullptr : w.F32, w.ld, w.piv, w.lu, s);
-      if (e) return e;
-      DeviceStatus h;
-      if ((e = read_status(w.lu.st, s, &h))) return e;
-      if (h.error) return h.error;
-      info->lu_info = h.lu_info;
-      info->t_factor_ms += t.stop();
-    }
     Timer t(s);
-    rhs_kernel<<<g, 256, 0, s>>>(q, p->N, n, w.dr, w.bs);
-    UPDES_LAUNCH_CHECK();
+    if (qstride == 1) {
+      rhs_kernel<<<g, 256, 0, s>>>(q, p->N, n, w.dr, w.bs);
+      UPDES_LAUNCH_CHECK();
+    } else {
+      UPDES_CUDA_TRY(cudaMemsetAsync(w.r, 0, size_t(n) * 8, s));
+      UPDES_CUDA_TRY(cudaMemcpy2DAsync(w.r, 8, q, qstride * 8, 8, p->N, cudaMemcpyDeviceToDevice, s));
+      rhs_kernel<<<g, 256, 0, s>>>(w.r, p->N, n, w.dr, w.bs);
+      UPDES_LAUNCH_CHECK();
+    }
     abs_kernel<<<g, 256, 0, s>>>(w.bs, w.bsabs, n);
     UPDES_LAUNCH_CHECK();
     UPDES_CUDA_TRY(cudaMemcpyAsync(w.x, w.bs, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
@@ -740,17 +818,154 @@ extern "C" int updes_solve(const updes_problem* p, const double* q, double* coef
     if (info->converged || !o.fallback_fp64) break;
     precision = UPDES_PREC_FP64;
     info->fell_back = 1;
+    if ((e = factor_stage(w, n, precision, info, s))) return e;
   }
-  // coeffs = dc .* x
-  {
-    Timer t(s);
-    axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.x, 0.0, n, w.dc);
-    UPDES_LAUNCH_CHECK();
+  Timer t(s);
+  axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.x, 0.0, n, w.dc);  // coeffs = dc .* x
+  UPDES_LAUNCH_CHECK();
+  if (cstride == 1) {
     UPDES_CUDA_TRY(cudaMemcpyAsync(coeffs, w.x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    if (vals && (e = updes_eval_values(p, coeffs, vals, stream))) return e;
-    info->t_eval_ms = t.stop();
+    if (vals && vstride == 1 && (e = updes_eval_values(p, coeffs, vals, s))) return e;
+  } else {
+    UPDES_CUDA_TRY(cudaMemcpy2DAsync(coeffs, cstride * 8, w.x, 8, 8, n, cudaMemcpyDeviceToDevice, s));
   }
+  if (vals && (cstride != 1 || vstride != 1)) {
+    if ((e = updes_eval_values(p, w.x, w.wv, s))) return e;
+    UPDES_CUDA_TRY(cudaMemcpy2DAsync(vals, vstride * 8, w.wv, 8, 8, p->N, cudaMemcpyDeviceToDevice, s));
+  }
+  info->t_eval_ms += t.stop();
+  return UPDES_OK;
+}
+
+int solve_setup(const updes_problem* p, const updes_solve_opts* opts, void* workspace, size_t workspace_bytes,
+                SolveWs* w, updes_solve_opts* o) {
+  if (updes_check_problem(p) || !workspace) return UPDES_ERR_INVALID;
+  *o = normalise(opts);
+  if (o->precision != UPDES_PREC_FP64 && o->precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
+  const int n = p->N + p->M;
+  updes_solve_opts olay = *o;
+  olay.precision = UPDES_PREC_FP32;
+  if (workspace_bytes < solve_ws_layout(n, olay, nullptr, nullptr)) return UPDES_ERR_WORKSPACE;
+  solve_ws_layout(n, olay, static_cast<char*>(workspace), w);
+  return UPDES_OK;
+}
+
+}  // namespace
+
+extern "C" int updes_factor(const updes_problem* p, const updes_solve_opts* opts, updes_solve_info* info,
+                            void* workspace, size_t workspace_bytes, void* stream) {
+  SolveWs w;
+  updes_solve_opts o;
+  int e = solve_setup(p, opts, workspace, workspace_bytes, &w, &o);
+  if (e) return e;
+  updes_solve_info dummy;
+  if (!info) info = &dummy;
+  std::memset(info, 0, sizeof *info);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int n = p->N + p->M;
+  if ((e = assemble_stage(p, w, n, info, s))) return e;
+  if ((e = factor_stage(w, n, o.precision, info, s))) return e;
+  return info->lu_info ? UPDES_ERR_SINGULAR : UPDES_OK;
+}
+
+extern "C" int updes_solve_factored(const updes_problem* p, int32_t nrhs, const double* Q, int64_t ldq,
+                                    double* coeffs, int64_t ldc, double* vals, int64_t ldv,
+                                    const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                                    size_t workspace_bytes, void* stream) {
+  SolveWs w;
+  updes_solve_opts o;
+  int e = solve_setup(p, opts, workspace, workspace_bytes, &w, &o);
+  if (e) return e;
+  if (nrhs <= 0 || !Q || !coeffs || ldq < nrhs || ldc < nrhs || (vals && ldv < nrhs)) return UPDES_ERR_INVALID;
+  updes_solve_info dummy;
+  if (!info) info = &dummy;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int n = p->N + p->M;
+  updes_solve_info agg;
+  std::memset(&agg, 0, sizeof agg);
+  agg.converged = 1;
+  for (int j = 0; j < nrhs; ++j) {
+    updes_solve_info one;
+    std::memset(&one, 0, sizeof one);
+    if ((e = solve_stage(p, w, n, Q + j, ldq, coeffs + j, ldc, vals ? vals + j : nullptr, ldv, o, &one, s))) return e;
+    agg.iters += one.iters;
+    agg.fell_back |= one.fell_back;
+    agg.lu_info = one.lu_info ? one.lu_info : agg.lu_info;
+    agg.converged &= one.converged;
+    agg.rel_residual = std::fmax(agg.rel_residual, one.rel_residual);
+    agg.backward_error = std::fmax(agg.backward_error, one.backward_error);
+    agg.t_factor_ms += one.t_factor_ms;
+    agg.t_refine_ms += one.t_refine_ms;
+    agg.t_eval_ms += one.t_eval_ms;
+  }
+  *info = agg;
+  return agg.converged ? UPDES_OK : UPDES_ERR_NOT_CONVERGED;
+}
+
+extern "C" int updes_solve(const updes_problem* p, const double* q, double* coeffs, double* vals,
+                           const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+  SolveWs w;
+  updes_solve_opts o;
+  int e = solve_setup(p, opts, workspace, workspace_bytes, &w, &o);
+  if (e) return e;
+  if (!q || !coeffs) return UPDES_ERR_INVALID;
+  updes_solve_info dummy;
+  if (!info) info = &dummy;
+  std::memset(info, 0, sizeof *info);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int n = p->N + p->M;
+  if ((e = assemble_stage(p, w, n, info, s))) return e;
+  if ((e = factor_stage(w, n, o.precision, info, s))) return e;
+  if ((e = solve_stage(p, w, n, q, 1, coeffs, 1, vals, 1, o, info, s))) return e;
   if (info->lu_info) return UPDES_ERR_SINGULAR;
   if (!info->converged) return UPDES_ERR_NOT_CONVERGED;
   return UPDES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint: K^T lambda = g with the factors left in the workspace by updes_solve
+// ---------------------------------------------------------------------------
+extern "C" int updes_solve_transpose(const updes_problem* p, const double* g, double* lambda,
+                                     const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  if (updes_check_problem(p) || !g || !lambda || !workspace) return UPDES_ERR_INVALID;
+  updes_solve_opts o = normalise(opts);
+  const int n = p->N + p->M;
+  updes_solve_opts olay = o;
+  olay.precision = UPDES_PREC_FP32;
+  if (workspace_bytes < solve_ws_layout(n, olay, nullptr, nullptr)) return UPDES_ERR_WORKSPACE;
+  SolveWs w;
+  solve_ws_layout(n, olay, static_cast<char*>(workspace), &w);
+  updes_solve_info dummy;
+  if (!info) info = &dummy;
+  std::memset(info, 0, sizeof *info);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int precision = 0;
+  if (int e0 = read_state(w, n, &precision, s)) return e0;  // no factorisation of this system in the workspace
+  const unsigned gr = unsigned(ceil_div(n, 256));
+  Timer t(s);
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.lu.st, 0, sizeof(DeviceStatus), s));
+  // K^T lambda = g  <=>  Ks^T mu = dc .* g,  lambda = dr .* mu
+  UPDES_CUDA_TRY(cudaMemcpyAsync(w.bs, g, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+  axpby_kernel<<<gr, 256, 0, s>>>(w.bs, 1.0, w.bs, 0.0, n, w.dc);
+  UPDES_LAUNCH_CHECK();
+  abs_kernel<<<gr, 256, 0, s>>>(w.bs, w.bsabs, n);
+  UPDES_LAUNCH_CHECK();
+  UPDES_CUDA_TRY(cudaMemcpyAsync(w.x, w.bs, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+  int e;
+  if ((e = precond(w, n, precision, w.x, s, true))) return e;
+  updes_solve_opts oi = o;
+  if (precision == UPDES_PREC_FP64) oi.max_iters = 0;
+  if ((e = gmres(w, n, precision, oi, info, s, true))) return e;
+  if (precision == UPDES_PREC_FP64) info->converged = 1;
+  info->fell_back = precision == UPDES_PREC_FP64 && o.precision == UPDES_PREC_FP32;
+  axpby_kernel<<<gr, 256, 0, s>>>(w.x, 1.0, w.x, 0.0, n, w.dr);
+  UPDES_LAUNCH_CHECK();
+  UPDES_CUDA_TRY(cudaMemcpyAsync(lambda, w.x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+  DeviceStatus h;
+  if ((e = read_status(w.lu.st, s, &h))) return e;
+  if (h.error) return h.error;
+  info->t_refine_ms = t.stop();
+  return info->converged ? UPDES_OK : UPDES_ERR_NOT_CONVERGED;
 }

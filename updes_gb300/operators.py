@@ -51,6 +51,7 @@ class SolverOptions:
     fallback_fp64: bool = True         # refactor in FP64 when refinement stalls
     compat_reference_quirks: bool = True
     self_term: bool = False            # True: keep phi(0) on the diagonal of the Phi blocks
+    reuse_factorization: bool = True   # reuse the last factors when the system (not the rhs) is unchanged
 
     def c_opts(self):
         o = _lib.SolveOpts()
@@ -425,8 +426,33 @@ def free_workspace():
     _WS_CACHE.clear()
 
 
-def solve_device(dp: DeviceProblem, q, opts: SolverOptions, want_vals=True):
-    """Run ``updes_solve`` on device tensors; returns (coeffs, vals, info dict)."""
+class _Factored:
+    """A factorised system kept on the device: its problem arrays and workspace."""
+
+    def __init__(self, key, dp, ws):
+        self.key, self.dp, self.ws = key, dp, ws
+
+
+_FACTOR_CACHE: dict = {}   # (device, slot) -> _Factored
+
+
+def _system_key(cloud, rbf, max_degree, W, kind, bnodes, geom, opts):
+    import hashlib
+    h = hashlib.sha1()
+    for a in (np.ascontiguousarray(cloud.sorted_nodes), np.ascontiguousarray(W), np.ascontiguousarray(kind),
+              np.ascontiguousarray(bnodes), np.ascontiguousarray(geom)):
+        h.update(a.tobytes())
+    return (rbf_spec(rbf), int(max_degree), opts.precision, bool(opts.self_term), h.hexdigest())
+
+
+def solve_device(dp: DeviceProblem, q, opts: SolverOptions, want_vals=True, key=None, slot="main"):
+    """Solve on device tensors; returns (coeffs, vals, info dict).
+
+    With ``key`` (a description of the system) the factorisation is cached per
+    device and ``slot``: a later call with the same key solves against the
+    stored factors (``updes_solve_factored``) instead of refactoring.
+    Without it every call is a fresh ``updes_solve``.
+    """
     torch = dp.torch
     lib = _lib.load()
     q = torch.as_tensor(q, dtype=torch.float64, device=dp.device).contiguous()
@@ -436,16 +462,45 @@ def solve_device(dp: DeviceProblem, q, opts: SolverOptions, want_vals=True):
     nbytes = ctypes.c_size_t()
     _lib.check(lib.updes_solve_workspace(ctypes.byref(dp.c), ctypes.byref(co), ctypes.byref(nbytes)),
                "updes_solve_workspace")
-    ws = workspace(nbytes.value)
     info = _lib.SolveInfo()
-    st = lib.updes_solve(ctypes.byref(dp.c), q.data_ptr(), coeffs.data_ptr(),
-                         vals.data_ptr() if vals is not None else None, ctypes.byref(co), ctypes.byref(info),
-                         ws.data_ptr(), ws.numel(), dp.stream())
+    if key is None:
+        ws = workspace(nbytes.value)
+        st = lib.updes_solve(ctypes.byref(dp.c), q.data_ptr(), coeffs.data_ptr(),
+                             vals.data_ptr() if vals is not None else None, ctypes.byref(co), ctypes.byref(info),
+                             ws.data_ptr(), ws.numel(), dp.stream())
+        what = "updes_solve"
+    else:
+        ck = (dp.device.index, slot)
+        ent = _FACTOR_CACHE.get(ck)
+        if ent is None or ent.key != key:
+            old = ent.ws if ent is not None and ent.ws.numel() >= nbytes.value else None
+            _FACTOR_CACHE.pop(ck, None)
+            ws = old if old is not None else torch.empty(nbytes.value, dtype=torch.uint8, device=dp.device)
+            fi = _lib.SolveInfo()
+            st = lib.updes_factor(ctypes.byref(dp.c), ctypes.byref(co), ctypes.byref(fi), ws.data_ptr(), ws.numel(),
+                                  dp.stream())
+            _lib.check(st, "updes_factor")
+            ent = _Factored(key, dp, ws)
+            _FACTOR_CACHE[ck] = ent
+        else:
+            fi = None
+        st = lib.updes_solve_factored(ctypes.byref(ent.dp.c), 1, q.data_ptr(), 1, coeffs.data_ptr(), 1,
+                                      vals.data_ptr() if vals is not None else None, 1, ctypes.byref(co),
+                                      ctypes.byref(info), ent.ws.data_ptr(), ent.ws.numel(), dp.stream())
+        if fi is not None:
+            info.t_assemble_ms, info.t_factor_ms = fi.t_assemble_ms, fi.t_factor_ms + info.t_factor_ms
+            info.lu_info = fi.lu_info
+        what = "updes_solve_factored"
     d = info.as_dict()
+    d["reused_factors"] = key is not None and fi is None
     LAST_INFO.clear()
     LAST_INFO.update(d)
-    _lib.check(st, "updes_solve")
+    _lib.check(st, what)
     return coeffs, vals, d
+
+
+def free_factorizations():
+    _FACTOR_CACHE.clear()
 
 
 def eval_field(points, coeffs, centers, rbf, what=0):
@@ -546,7 +601,11 @@ def core_compute_coefficients(field, cloud, rbf, nb_monomials, options=None):
     deg = {1: 0, 3: 1, 6: 2, 10: 3, 15: 4}[nb_monomials]
     dp = _interp_problem(cloud, rbf, deg)
     o = options or SolverOptions(precision="fp64")
-    coeffs, _, _ = solve_device(dp, np.asarray(field, dtype=np.float64), o, want_vals=False)
+    key = None
+    if o.reuse_factorization:
+        key = ("interp",) + _system_key(cloud, rbf, deg, np.zeros((0, 5)), np.zeros(0, np.int32),
+                                        np.zeros((0, 2), np.int32), np.zeros((0, 8)), o)
+    coeffs, _, _ = solve_device(dp, np.asarray(field, dtype=np.float64), o, want_vals=False, key=key, slot="interp")
     return coeffs.cpu().numpy()
 
 
@@ -636,7 +695,8 @@ def pde_solver(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max
     W, kind, bnodes, geom, q = prepare(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max_degree,
                                        diff_args, rhs_args, opts)
     dp = DeviceProblem(cloud, rbf, max_degree, W, kind, bnodes, geom, opts.self_term)
-    coeffs, vals, _ = solve_device(dp, q, opts)
+    key = _system_key(cloud, rbf, max_degree, W, kind, bnodes, geom, opts) if opts.reuse_factorization else None
+    coeffs, vals, _ = solve_device(dp, q, opts, key=key)
     coeffs_h = coeffs.cpu().numpy()
     vals_h = vals.cpu().numpy()
 
