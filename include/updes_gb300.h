@@ -39,7 +39,8 @@ enum {
   UPDES_ERR_NOT_CONVERGED = 4,  /* refinement stalled or hit its iteration cap   */
   UPDES_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up            */
   UPDES_ERR_UNSUPPORTED = 6,    /* valid request this build does not implement   */
-  UPDES_ERR_WORKSPACE = 7       /* workspace too small                           */
+  UPDES_ERR_WORKSPACE = 7,      /* workspace too small                           */
+  UPDES_ERR_TOO_LARGE = 8       /* beyond the fixed scratch of updes_lu_solve_noalloc */
 };
 
 /* ---- radial basis functions (updes/utils.py:30-69) --------------------- */
@@ -164,6 +165,31 @@ UPDES_API int updes_lu_factor(int32_t n, double* A, int64_t lda, int32_t precisi
 UPDES_API int updes_lu_solve(int32_t n, const void* F, int64_t ldf, int32_t precision, const int32_t* piv, double* b,
                    int32_t nrhs, int64_t ldb, int32_t trans, void* workspace, size_t workspace_bytes,
                    void* stream);
+
+/*
+ * updes_lu_solve without any device allocation or caller workspace.
+ *
+ * No counterpart in the reference.  It exists for callers that are not
+ * allowed to allocate device memory at the point where they solve: a handler
+ * run by another framework's executor (an XLA custom call, for instance,
+ * receives only the buffers the framework planned and must not allocate
+ * behind its back), or a time-stepping loop that has to stay off the
+ * allocator.  They pass the factors, pivots and right-hand sides as for
+ * updes_lu_solve; the scratch (a status word, the triangular solves' block
+ * flags and two n-vectors) is a fixed array inside the library, about 387 KB
+ * on every GPU that loads it, kept until the process exits.
+ *
+ * Limit: n <= UPDES_NOALLOC_MAX_N; larger n returns UPDES_ERR_TOO_LARGE before
+ * any GPU work.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current, so make that
+ * first call before any stream capture.  Every call on a device shares the
+ * same array: calls that overlap on the GPU (different streams, or different
+ * host threads) race, so order them, e.g. on one stream.  Each call clears
+ * the parts that must start at zero itself.
+ */
+#define UPDES_NOALLOC_MAX_N 24576
+UPDES_API int updes_lu_solve_noalloc(int32_t n, const void* F, int64_t ldf, int32_t precision, const int32_t* piv,
+                                     double* b, int32_t nrhs, int64_t ldb, int32_t trans, void* stream);
 
 /* r = b - K x (trans = 0) or r = b - K^T x (trans = 1) with FP64 K, x, b, r (device, n). */
 UPDES_API int updes_residual(int32_t n, const double* K, int64_t ldk, const double* x, const double* b,

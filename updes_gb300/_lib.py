@@ -13,7 +13,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libupdes_gb300.so")
 
 # status codes
-OK, ERR_INVALID, ERR_CUDA, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_WORKSPACE = range(8)
+OK, ERR_INVALID, ERR_CUDA, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_WORKSPACE, \
+    ERR_TOO_LARGE = range(9)
+NOALLOC_MAX_N = 24576  # UPDES_NOALLOC_MAX_N
 # kernels
 RBF_POLYHARMONIC, RBF_GAUSSIAN, RBF_MULTIQUADRIC, RBF_INVERSE_MULTIQUADRIC, RBF_THIN_PLATE = range(5)
 # boundary rows
@@ -90,6 +92,7 @@ SIGNATURES = {
     "updes_lu_factor": (ctypes.c_int, [_i32, _vp, _i64, _i32, _vp, _i64, _vp, _vp, _sz,
                                        ctypes.POINTER(_i32), _vp]),
     "updes_lu_solve": (ctypes.c_int, [_i32, _vp, _i64, _i32, _vp, _vp, _i32, _i64, _i32, _vp, _sz, _vp]),
+    "updes_lu_solve_noalloc": (ctypes.c_int, [_i32, _vp, _i64, _i32, _vp, _vp, _i32, _i64, _i32, _vp]),
     "updes_residual": (ctypes.c_int, [_i32, _vp, _i64, _vp, _vp, _vp, _i32, _vp]),
     "updes_solve_workspace": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(_sz)]),

@@ -266,6 +266,7 @@ extern "C" const char* updes_status_string(int status) {
     case UPDES_ERR_TIMEOUT: return "a bounded device-side wait timed out";
     case UPDES_ERR_UNSUPPORTED: return "unsupported by this build";
     case UPDES_ERR_WORKSPACE: return "workspace too small";
+    case UPDES_ERR_TOO_LARGE: return "n exceeds UPDES_NOALLOC_MAX_N, the fixed scratch of updes_lu_solve_noalloc";
     default: return "unknown status";
   }
 }
@@ -921,6 +922,71 @@ extern "C" int updes_solve(const updes_problem* p, const double* q, double* coef
   if (info->lu_info) return UPDES_ERR_SINGULAR;
   if (!info->converged) return UPDES_ERR_NOT_CONVERGED;
   return UPDES_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solves with a fixed, library-owned scratch (no allocation at all)
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocSyncOff = 256;                                   // after the status word
+constexpr size_t kNoallocVecOff = 2304;                                   // after (n/64 + 2) flags
+constexpr size_t kNoallocBytes = kNoallocVecOff + 2 * size_t(UPDES_NOALLOC_MAX_N) * sizeof(double);
+static_assert(kNoallocVecOff - kNoallocSyncOff >= sizeof(int) * (UPDES_NOALLOC_MAX_N / 64 + 2), "flag region");
+
+// The only scratch of updes_lu_solve_noalloc, shared by all its calls on a device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once per device).
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  UPDES_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return UPDES_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    UPDES_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return UPDES_OK;
+}
+
+}  // namespace
+
+extern "C" int updes_lu_solve_noalloc(int32_t n, const void* F, int64_t ldf, int32_t precision, const int32_t* piv,
+                                      double* b, int32_t nrhs, int64_t ldb, int32_t trans, void* stream) {
+  if (n <= 0 || !F || ldf < n || !piv || !b || nrhs <= 0 || ldb < nrhs) return UPDES_ERR_INVALID;
+  if (precision != UPDES_PREC_FP64 && precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
+  if (n > UPDES_NOALLOC_MAX_N) return UPDES_ERR_TOO_LARGE;
+  void* base = nullptr;
+  int e = noalloc_scratch(&base);
+  if (e) return e;
+  char* c = static_cast<char*>(base);
+  LuWs w{};
+  w.st = reinterpret_cast<DeviceStatus*>(c);
+  w.sync = reinterpret_cast<int*>(c + kNoallocSyncOff);
+  w.tmp = reinterpret_cast<double*>(c + kNoallocVecOff);
+  double* col = w.tmp + UPDES_NOALLOC_MAX_N;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DeviceStatus), s));  // the flags are cleared by each solve
+  for (int j = 0; j < nrhs; ++j) {
+    double* bj = b + j;
+    if (nrhs == 1) {
+      if ((e = solve_any(n, F, ldf, precision, piv, bj, trans, w, s))) return e;
+      continue;
+    }
+    UPDES_CUDA_TRY(cudaMemcpy2DAsync(col, 8, bj, ldb * 8, 8, n, cudaMemcpyDeviceToDevice, s));
+    if ((e = solve_any(n, F, ldf, precision, piv, col, trans, w, s))) return e;
+    UPDES_CUDA_TRY(cudaMemcpy2DAsync(bj, ldb * 8, col, 8, 8, n, cudaMemcpyDeviceToDevice, s));
+  }
+  DeviceStatus h;
+  if ((e = read_status(w.st, s, &h))) return e;
+  return h.error;
 }
 
 // ---------------------------------------------------------------------------
