@@ -249,6 +249,39 @@ UPDES_API int updes_solve_factored(const updes_problem* p, int32_t nrhs, const d
                                    const updes_solve_opts* opts, updes_solve_info* info, void* workspace,
                                    size_t workspace_bytes, void* stream);
 
+/*
+ * Batched right-hand sides with a fixed number of refinement sweeps.  R <= 64
+ * columns of the row-major N x R block Q (ldq) are solved together against the
+ * factors that updes_factor left in `workspace`: X = M^-1 Q, then `sweeps`
+ * times X += M^-1 (Q - K X), with the residual and the triangular solves in
+ * double-float arithmetic; coeffs (n x R, ldc) receives X.  FP64 factors
+ * (precision UPDES_PREC_FP64) give M^-1 the accuracy of an FP64 solve, so one
+ * sweep reaches FP64 quality; FP32 factors converge only as fast as classical
+ * refinement on them allows.
+ * updes_batch_prepare (once per factorisation; synchronises) derives the
+ * batch's copy of the factors.  updes_solve_batch then only launches kernels on
+ * `stream`: no synchronisation and no host reads, so a time step built from it
+ * can be captured in a CUDA graph.  A stale or missing preparation, and any
+ * timed-out wait, land in the workspace's status word, which
+ * updes_workspace_status reads and clears.
+ * batch_ws: scratch of updes_batch_workspace(n) bytes.
+ * The reference solves each right-hand side with a full rebuild
+ * (demos/Advection/00_advection_with_rbf.py:83-93).
+ */
+UPDES_API int updes_batch_workspace(int32_t n, size_t* bytes);
+UPDES_API int updes_batch_prepare(const updes_problem* p, void* workspace, size_t workspace_bytes, void* batch_ws,
+                                  size_t batch_ws_bytes, void* stream);
+UPDES_API int updes_solve_batch(const updes_problem* p, int32_t R, const double* Q, int64_t ldq, double* coeffs,
+                                int64_t ldc, int32_t sweeps, void* workspace, size_t workspace_bytes,
+                                void* batch_ws, size_t batch_ws_bytes, void* stream);
+UPDES_API int updes_workspace_status(const updes_problem* p, void* workspace, size_t workspace_bytes,
+                                     int32_t* error, void* stream);
+
+/* vals (N x R, ldv) = [Phi P] C for coefficient columns C (n x R, ldc), R <= 64: the batched
+ * counterpart of updes_eval_values (kernel values regenerated once per pair, shared by the columns). */
+UPDES_API int updes_eval_values_batch(const updes_problem* p, int32_t R, const double* C, int64_t ldc, double* vals,
+                                      int64_t ldv, void* stream);
+
 /* ---- adjoint (reverse mode through the solve) ------------------------------
  * The reference differentiates pde_solver with jax.grad through inv, the GEMM
  * and the lineax QR (demos/Laplace/10_laplace_with_diff_phys.py:89-104) or runs

@@ -52,18 +52,38 @@ def test_adjoint_matches_reference_autodiff(precision):
 
 
 def test_adjoint_matches_central_differences():
-    """Directional derivatives along random directions, central differences with h = 1e-6."""
+    """Directional derivatives along random directions against central differences.
+
+    The boundary-control workload solves in FP64, so the quotients are taken on the FP64 path.  J is
+    exactly quadratic in the control, so h = 1e-2 is exact up to rounding and pins the adjoint at 1e-8.
+    At h = 1e-6 the quotient carries the forward solve's rounding divided by 2h: along the control the
+    factors are reused and that noise is about 1e-6 of the derivative (bound 1e-5); along the fields K
+    itself changes and is refactored, whose rounding (about 1e-11 of J on this r^5 system) gives about
+    1e-4 of the derivative (bound 1e-3).  At h = 1e-4 the fields' quotient is pinned at 1e-6 (O(h^2)
+    truncation).  The FP32 path's adjoint is checked along the control at h = 1e-2.
+    """
     g = load("adjoint_kgrad_10x10")
     case = C.CASES[C.ADJOINT_CASE]
     cl = product_cloud(case)
     F0 = C.make_fields(case, cl.sorted_nodes)
     c0 = g["control"]
-    J, dc, dF = _loss("fp32")
     rng = np.random.default_rng(0)
-    h = 1e-6
     v = rng.standard_normal(c0.shape)
-    fd = (_loss("fp32", control=c0 + h * v, want_grad=False) - _loss("fp32", control=c0 - h * v, want_grad=False)) / (2 * h)
-    assert abs(fd - dc @ v) <= 1e-6 * abs(dc @ v) + 1e-12
     V = rng.standard_normal(F0.shape)
-    fd = (_loss("fp32", fields=F0 + h * V, want_grad=False) - _loss("fp32", fields=F0 - h * V, want_grad=False)) / (2 * h)
-    assert abs(fd - np.sum(dF * V)) <= 1e-6 * abs(np.sum(dF * V)) + 1e-12
+
+    def fd_c(prec, h):
+        return (_loss(prec, control=c0 + h * v, want_grad=False) -
+                _loss(prec, control=c0 - h * v, want_grad=False)) / (2 * h)
+
+    def fd_f(prec, h):
+        return (_loss(prec, fields=F0 + h * V, want_grad=False) -
+                _loss(prec, fields=F0 - h * V, want_grad=False)) / (2 * h)
+
+    J, dc, dF = _loss("fp64")
+    gc, gf = dc @ v, np.sum(dF * V)
+    assert abs(fd_c("fp64", 1e-2) - gc) <= 1e-8 * abs(gc)
+    assert abs(fd_c("fp64", 1e-6) - gc) <= 1e-5 * abs(gc)
+    assert abs(fd_f("fp64", 1e-4) - gf) <= 1e-6 * abs(gf)
+    assert abs(fd_f("fp64", 1e-6) - gf) <= 1e-3 * abs(gf)
+    J32, dc32, _ = _loss("fp32")
+    assert abs(fd_c("fp32", 1e-2) - dc32 @ v) <= 1e-8 * abs(dc32 @ v)

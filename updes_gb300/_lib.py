@@ -102,6 +102,12 @@ SIGNATURES = {
                                     _vp, _sz, _vp]),
     "updes_solve_factored": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _i64, _vp, _i64, _vp, _i64,
                                             ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),
+    "updes_batch_workspace": (ctypes.c_int, [_i32, ctypes.POINTER(_sz)]),
+    "updes_batch_prepare": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _sz, _vp, _sz, _vp]),
+    "updes_solve_batch": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _i64, _vp, _i64, _i32, _vp, _sz, _vp,
+                                         _sz, _vp]),
+    "updes_workspace_status": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _sz, ctypes.POINTER(_i32), _vp]),
+    "updes_eval_values_batch": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _i64, _vp, _i64, _vp]),
     "updes_eval_values_t": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp]),
     "updes_solve_transpose": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),

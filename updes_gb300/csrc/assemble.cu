@@ -372,6 +372,86 @@ __global__ void pt_matvec_kernel(updes_problem p, const double* __restrict__ g, 
   }
 }
 
+// vals[i][c] = sum_{j != i} phi(x_i - x_j) C[j][c] + sum_k m_k(x_i) C[N+k][c] for R <= 64 columns: phi is
+// evaluated once per pair in FP64 and applied to every column in double-float (FP32 ALU).
+constexpr int kEvBRows = 16;
+template <int KIND>
+__global__ void __launch_bounds__(256) eval_values_batch_kernel(updes_problem p, int R, const double* __restrict__ C,
+                                                                int64_t ldc, double* __restrict__ vals, int64_t ldv) {
+  __shared__ double sx[64], sy[64];
+  __shared__ float sch[64][65], scl[64][65];
+  __shared__ float sph[kEvBRows][65], spl[kEvBRows][65];
+  const int tid = threadIdx.x;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int r0 = blockIdx.x * kEvBRows;
+  // thread owns row tid / 16 and columns (tid % 16) * 4 + {0..3}
+  const int ty = tid >> 4, tx = tid & 15;
+  float ah[1][4] = {}, al[1][4] = {};
+  for (int j0 = 0; j0 < p.N; j0 += 64) {
+    __syncthreads();
+    for (int e = tid; e < 64; e += blockDim.x) {
+      const int j = j0 + e;
+      sx[e] = j < p.N ? p.nodes[2 * j] : 0.0;
+      sy[e] = j < p.N ? p.nodes[2 * j + 1] : 0.0;
+    }
+    for (int e = tid; e < 64 * 64; e += blockDim.x) {
+      const int jj = e >> 6, c = e & 63;
+      const double v = (j0 + jj < p.N && c < R) ? C[int64_t(j0 + jj) * ldc + c] : 0.0;
+      const float h = float(v);
+      sch[jj][c] = h;
+      scl[jj][c] = float(v - double(h));
+    }
+    __syncthreads();
+    for (int e = tid; e < kEvBRows * 64; e += blockDim.x) {
+      const int ii = e >> 6, jj = e & 63;
+      const int i = r0 + ii, j = j0 + jj;
+      double v = 0.0;
+      if (i < p.N && j < p.N && (j != i || p.self_term)) {
+        const double xi = p.nodes[2 * i], yi = p.nodes[2 * i + 1];
+        v = rbf_value<KIND>(xi - sx[jj], yi - sy[jj], p.rbf_param, ip);
+      }
+      const float h = float(v);
+      sph[ii][jj] = h;
+      spl[ii][jj] = float(v - double(h));
+    }
+    __syncthreads();
+    for (int jj = 0; jj < 64; ++jj) {
+#pragma unroll
+      for (int u = 0; u < 1; ++u) {
+        const float a = sph[ty + u][jj], a2 = spl[ty + u][jj];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int c = tx * 4 + v;
+          const float b = sch[jj][c], b2 = scl[jj][c];
+          // (ah, al) += (a + a2)(b + b2) in double-float, renormalised after every term
+          const float pr = __fmul_rn(a, b);
+          const float er = __fmaf_rn(a, b, -pr);
+          const float s = __fadd_rn(ah[u][v], pr);
+          const float bb = __fsub_rn(s, ah[u][v]);
+          float t = __fadd_rn(__fsub_rn(ah[u][v], __fsub_rn(s, bb)), __fsub_rn(pr, bb));
+          t = __fadd_rn(t, __fadd_rn(al[u][v], __fmaf_rn(a, b2, __fmaf_rn(a2, b, er))));
+          ah[u][v] = __fadd_rn(s, t);
+          al[u][v] = __fsub_rn(t, __fsub_rn(ah[u][v], s));
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 1; ++u) {
+    const int i = r0 + ty + u;
+    if (i >= p.N) continue;
+    const double xi = p.nodes[2 * i], yi = p.nodes[2 * i + 1];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int c = tx * 4 + v;
+      if (c >= R) continue;
+      double s = double(ah[u][v]) + double(al[u][v]);
+      for (int k = 0; k < p.M; ++k) s += monomial_terms(k, xi, yi).m * C[int64_t(p.N + k) * ldc + c];
+      vals[int64_t(i) * ldv + c] = s;
+    }
+  }
+}
+
 int check_problem(const updes_problem* p) {
   if (!p || p->N <= 0 || p->Ni < 0 || p->Ni > p->N) return UPDES_ERR_INVALID;
   if (!(p->M == 1 || p->M == 3 || p->M == 6 || p->M == 10 || p->M == 15)) return UPDES_ERR_INVALID;
@@ -490,6 +570,24 @@ extern "C" int updes_eval_values_t(const updes_problem* p, const double* g, doub
   }
   UPDES_LAUNCH_CHECK();
   pt_matvec_kernel<<<1, 1024, 0, s>>>(*p, g, out);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+extern "C" int updes_eval_values_batch(const updes_problem* p, int32_t R, const double* C, int64_t ldc, double* vals,
+                                       int64_t ldv, void* stream) {
+  int st = check_problem(p);
+  if (st) return st;
+  if (!C || !vals || R <= 0 || R > 64 || ldc < R || ldv < R) return UPDES_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const unsigned grid = unsigned(ceil_div(p->N, kEvBRows));
+  switch (p->rbf) {
+    case UPDES_RBF_POLYHARMONIC: eval_values_batch_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, R, C, ldc, vals, ldv); break;
+    case UPDES_RBF_GAUSSIAN: eval_values_batch_kernel<UPDES_RBF_GAUSSIAN><<<grid, 256, 0, s>>>(*p, R, C, ldc, vals, ldv); break;
+    case UPDES_RBF_MULTIQUADRIC: eval_values_batch_kernel<UPDES_RBF_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, R, C, ldc, vals, ldv); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC: eval_values_batch_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, R, C, ldc, vals, ldv); break;
+    default: eval_values_batch_kernel<UPDES_RBF_THIN_PLATE><<<grid, 256, 0, s>>>(*p, R, C, ldc, vals, ldv); break;
+  }
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }

@@ -37,9 +37,10 @@ static_assert(kGroups * TN <= int(kTmemCols), "accumulators must fit in tensor m
 constexpr int kATile = TM * TK * 2;  // 16 KB per digit plane
 constexpr int kBTile = TN * TK * 2;  //  8 KB per digit plane
 constexpr int kSmemOperands = kDigits * (kATile + kBTile);
-// 120 KB: more than half of an SM's shared memory, so one CTA per SM (it owns 512 TMEM columns)
-constexpr int kSmemBytes = 120 * 1024;
-static_assert(kSmemOperands + 1024 + 1024 + 64 <= kSmemBytes, "shared memory layout");
+// two operand buffers + scales + partial maxima; more than half of an SM's shared memory, so one CTA per
+// SM (it owns 512 TMEM columns)
+constexpr int kSmemBytes = 2 * kSmemOperands + 1024 /*align*/ + 2 * (TM + TN) * 4 + 16 * TN * 4 + 64;
+static_assert(kSmemBytes > 116 * 1024 && kSmemBytes <= 227 * 1024, "shared memory layout");
 
 // instruction descriptor: D = F32, A = B = BF16, both K-major, N = 64, M = 128
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TM >> 4) << 24);
@@ -120,12 +121,39 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase)
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+template <bool ACC>
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "n"(ACC ? 1 : 0)
       : "memory");
+}
+
+// Digit product (A, B) over the four k-steps of a block into group A + B.  The descriptors are built once
+// per buffer and every operand offset is a compile-time constant (descriptor units of 16 bytes), so the
+// issuing thread keeps pace with the tensor pipe.
+template <int A, int B>
+__device__ __forceinline__ void mma_product(uint32_t tmem, uint64_t a0, uint64_t b0) {
+  constexpr int g = A + B;
+  constexpr bool first = (A == (g >= kDigits ? g - kDigits + 1 : 0));  // the group's first product
+  const uint32_t d = tmem + uint32_t(g * TN);
+#pragma unroll
+  for (int kk = 0; kk < TK / 16; ++kk) {
+    const uint64_t ad = a0 + uint64_t(A * (kATile >> 4) + kk * 2), bd = b0 + uint64_t(B * (kBTile >> 4) + kk * 2);
+    if (first && kk == 0) mma_bf16<false>(d, ad, bd);
+    else mma_bf16<true>(d, ad, bd);
+  }
+}
+
+// all D x D products, a-major (so each group's first product is issued first)
+template <int A, int B>
+__device__ __forceinline__ void mma_all(uint32_t tmem, uint64_t a0, uint64_t b0) {
+  if constexpr (A < kDigits) {
+    mma_product<A, B>(tmem, a0, b0);
+    if constexpr (B + 1 < kDigits) mma_all<A, B + 1>(tmem, a0, b0);
+    else mma_all<A + 1, 0>(tmem, a0, b0);
+  }
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -147,23 +175,130 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Global -> register staging of one 64-wide k block: A rows (4 x 8 values per thread) and B (16 values).
+struct Stage {
+  float4 a[4][2];
+  float4 b[4];
+};
+
+__device__ __forceinline__ void stage_load(Stage& st, const float* __restrict__ A, int64_t lda,
+                                           const float* __restrict__ B, int64_t ldb, int r0, int c0, int m, int nc,
+                                           int K, int kb, int tid, bool vec_ok) {
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const int chunk = tid + it * kThreads;  // 1024 chunks of 8 k values: row = chunk / 8
+    const int row = chunk >> 3, kc = chunk & 7;
+    const int gr = r0 + row, k0 = kb + kc * 8;
+    if (vec_ok && gr < m && k0 + 7 < K) {
+      const float4* p = reinterpret_cast<const float4*>(A + int64_t(gr) * lda + k0);
+      st.a[it][0] = __ldg(p);
+      st.a[it][1] = __ldg(p + 1);
+    } else {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = (gr < m && k0 + u < K) ? A[int64_t(gr) * lda + k0 + u] : 0.f;
+      st.a[it][0] = make_float4(v[0], v[1], v[2], v[3]);
+      st.a[it][1] = make_float4(v[4], v[5], v[6], v[7]);
+    }
+  }
+  // B: thread owns 4 consecutive columns j4..j4+3 and 4 consecutive k rows kq*4..kq*4+3
+  const int j4 = (tid & 15) * 4, kq = tid >> 4;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int k = kb + kq * 4 + u, gc = c0 + j4;
+    if (vec_ok && k < K && gc + 3 < nc) {
+      st.b[u] = __ldg(reinterpret_cast<const float4*>(B + int64_t(k) * ldb + gc));
+    } else {
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = (k < K && gc + q < nc) ? B[int64_t(k) * ldb + gc + q] : 0.f;
+      st.b[u] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+  }
+}
+
+__device__ __forceinline__ float f4(const float4& v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
+
+// Digits of a staged block into one shared-memory buffer (A: row scales, B: column scales).
+__device__ __forceinline__ void stage_digits(const Stage& st, uint8_t* sA, uint8_t* sB, float* sSA, float* sSB,
+                                             float* sBmax, int tid) {
+#pragma unroll
+  for (int it = 0; it < 4; ++it) {
+    const int chunk = tid + it * kThreads;
+    const int row = chunk >> 3, kc = chunk & 7;
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) { v[u] = f4(st.a[it][0], u); v[4 + u] = f4(st.a[it][1], u); }
+    float mx = 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(v[u]));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 4));
+    const int e = exp_of(mx);
+    if (kc == 0) sSA[row] = pow2f(e - 8);
+    const float scale = pow2f(8 - e);
+    __align__(16) __nv_bfloat16 d[kDigits][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      float dd[kDigits];
+      digits(v[u], scale, dd);
+#pragma unroll
+      for (int p = 0; p < kDigits; ++p) d[p][u] = __float2bfloat16_rn(dd[p]);
+    }
+    const uint32_t off = sw128(row, kc * 8);
+#pragma unroll
+    for (int p = 0; p < kDigits; ++p) *reinterpret_cast<uint4*>(sA + p * kATile + off) = *reinterpret_cast<uint4*>(d[p]);
+  }
+  const int j4 = (tid & 15) * 4, kq = tid >> 4;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float mx = 0.f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) mx = fmaxf(mx, fabsf(f4(st.b[u], q)));
+    sBmax[kq * TN + j4 + q] = mx;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = j4 + q;
+    float mx = 0.f;
+    for (int w = 0; w < 16; ++w) mx = fmaxf(mx, sBmax[w * TN + j]);
+    const int e = exp_of(mx);
+    if (kq == 0) sSB[j] = pow2f(e - 8);
+    const float scale = pow2f(8 - e);
+    __align__(8) __nv_bfloat16 d[kDigits][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float dd[kDigits];
+      digits(f4(st.b[u], q), scale, dd);
+#pragma unroll
+      for (int p = 0; p < kDigits; ++p) d[p][u] = __float2bfloat16_rn(dd[p]);
+    }
+    const uint32_t off = sw128(j, kq * 4);
+#pragma unroll
+    for (int p = 0; p < kDigits; ++p) *reinterpret_cast<uint2*>(sB + p * kBTile + off) = *reinterpret_cast<uint2*>(d[p]);
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki_update_kernel(float* __restrict__ Chi, float* __restrict__ Clo, int64_t ldc, const float* __restrict__ A,
                         int64_t lda, const float* __restrict__ B, int64_t ldb, int m, int nc, int K,
                         DeviceStatus* st) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* sA = smem;                              // 3 x 16 KB
-  uint8_t* sB = smem + kDigits * kATile;           // 3 x 8 KB
-  float* sSA = reinterpret_cast<float*>(smem + kSmemOperands);  // 128 row scales 2^(eA-8)
-  float* sSB = sSA + TM;                                        // 64 column scales 2^(eB-8)
-  float* sBmax = sSB + TN;                                      // 4 x 64 partial column maxima
+  // two buffers of digit planes: [buf][A planes | B planes]
+  uint8_t* sOps[2] = {smem, smem + kSmemOperands};
+  float* sScale = reinterpret_cast<float*>(smem + 2 * kSmemOperands);  // [buf][128 row + 64 col]
+  float* sBmax = sScale + 2 * (TM + TN);                                 // 16 x 64 partial column maxima
   __shared__ uint64_t mbar;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_fail;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.y * TM, c0 = blockIdx.x * TN;
+  const bool vec_ok = ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15) == 0 &&
+                      (lda & 3) == 0 && (ldb & 3) == 0;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -176,105 +311,46 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_fail = 0;
   }
+  Stage stg;
+  stage_load(stg, A, lda, B, ldb, r0, c0, m, nc, K, 0, tid, vec_ok);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
-  uint32_t phase = 0, failed_phase = 0;
+  stage_digits(stg, sOps[0], sOps[0] + kDigits * kATile, sScale, sScale + TM, sBmax, tid);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
 
-  for (int kb = 0; kb < K; kb += TK) {
-    // ---- A: 128 rows x 64 k, row max over the block, 3 digit planes ----
-#pragma unroll 1
-    for (int it = 0; it < 4; ++it) {
-      const int chunk = tid + it * kThreads;  // 1024 chunks of 8 k-values
-      const int row = chunk >> 3, kc = chunk & 7;
-      float v[8];
-      const int gr = r0 + row;
+  // this thread's row and 32 columns of the result, accumulated in double-float over all k blocks
+  const int row = (warp & 3) * 32 + lane;
+  const int colbase = (warp >> 2) * 32;
+  const uint32_t lane_base = uint32_t((warp & 3) * 32) << 16;
+  float acc_h[32], acc_l[32];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int k = kb + kc * 8 + u;
-        v[u] = (gr < m && k < K) ? A[int64_t(gr) * lda + k] : 0.f;
-      }
-      float mx = 0.f;
-#pragma unroll
-      for (int u = 0; u < 8; ++u) mx = fmaxf(mx, fabsf(v[u]));
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 4));
-      const int e = exp_of(mx);
-      if (kc == 0) sSA[row] = pow2f(e - 8);
-      const float scale = pow2f(8 - e);
-      __align__(16) __nv_bfloat16 d[kDigits][8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        float dd[kDigits];
-        digits(v[u], scale, dd);
-#pragma unroll
-        for (int p = 0; p < kDigits; ++p) d[p][u] = __float2bfloat16_rn(dd[p]);
-      }
-      const uint32_t off = sw128(row, kc * 8);
-#pragma unroll
-      for (int p = 0; p < kDigits; ++p)
-        *reinterpret_cast<uint4*>(sA + p * kATile + off) = *reinterpret_cast<uint4*>(d[p]);
-    }
-    // ---- B: 64 k x 64 columns, column max, stored transposed (row = column j, K-major) ----
-    {
-      const int j = tid & 63, kq = tid >> 6;  // 4 quarters of 16 k
-      const int gc = c0 + j;
-      float v[16];
-      float mx = 0.f;
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int k = kb + kq * 16 + u;
-        v[u] = (gc < nc && k < K) ? B[int64_t(k) * ldb + gc] : 0.f;
-        mx = fmaxf(mx, fabsf(v[u]));
-      }
-      sBmax[kq * TN + j] = mx;
-      __syncthreads();
-      mx = fmaxf(fmaxf(sBmax[j], sBmax[TN + j]), fmaxf(sBmax[2 * TN + j], sBmax[3 * TN + j]));
-      const int e = exp_of(mx);
-      if (kq == 0) sSB[j] = pow2f(e - 8);
-      const float scale = pow2f(8 - e);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        __align__(16) __nv_bfloat16 d[kDigits][8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          float dd[kDigits];
-          digits(v[h * 8 + u], scale, dd);
-#pragma unroll
-          for (int p = 0; p < kDigits; ++p) d[p][u] = __float2bfloat16_rn(dd[p]);
-        }
-        const uint32_t off = sw128(j, kq * 16 + h * 8);
-#pragma unroll
-        for (int p = 0; p < kDigits; ++p)
-          *reinterpret_cast<uint4*>(sB + p * kBTile + off) = *reinterpret_cast<uint4*>(d[p]);
-      }
-    }
-    // generic-proxy smem writes -> visible to the tensor core (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    // ---- kDigits^2 digit products x 4 k-steps into kGroups accumulators ----
+  for (int u = 0; u < 32; ++u) { acc_h[u] = 0.f; acc_l[u] = 0.f; }
+
+  uint32_t phase = 0, failed_phase = 0;
+  const int nsub = int(ceil_div(K, TK));
+  for (int sb = 0; sb < nsub; ++sb) {
+    const int buf = sb & 1;
+    uint8_t* sA = sOps[buf];
+    uint8_t* sB = sOps[buf] + kDigits * kATile;
+    // ---- issue kDigits^2 digit products x 4 k-steps into kGroups accumulators ----
     if (tid == 0) {
       tc_fence_after();
-      bool started[kGroups] = {};
-#pragma unroll 1
-      for (int a = 0; a < kDigits; ++a) {
-#pragma unroll 1
-        for (int b = 0; b < kDigits; ++b) {
-          const int g = a + b;
-          const uint32_t d_tmem = tmem + uint32_t(g * TN);
-          const uint32_t abase = smem_u32(sA + a * kATile), bbase = smem_u32(sB + b * kBTile);
-#pragma unroll
-          for (int kk = 0; kk < TK / 16; ++kk) {
-            mma_bf16(d_tmem, make_desc(abase + kk * 32), make_desc(bbase + kk * 32), started[g] ? 1u : 0u);
-            started[g] = true;
-          }
-        }
-      }
+      // products in order of a; the first product of group g = a + b is (max(0, g - D + 1), ...)
+      mma_all<0, 0>(tmem, make_desc(smem_u32(sA)), make_desc(smem_u32(sB)));
       mma_commit(&mbar);
     }
     __syncwarp();
+    // ---- meanwhile: stage and digitise the next k block into the other buffer ----
+    if (sb + 1 < nsub) {
+      stage_load(stg, A, lda, B, ldb, r0, c0, m, nc, K, (sb + 1) * TK, tid, vec_ok);
+      uint8_t* nA = sOps[buf ^ 1];
+      float* nS = sScale + (buf ^ 1) * (TM + TN);
+      stage_digits(stg, nA, nA + kDigits * kATile, nS, nS + TM, sBmax, tid);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     // ---- wait for the accumulators ----
     if (!mbar_wait_bounded(&mbar, phase)) {
       s_fail = 1;
@@ -284,54 +360,78 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     __syncthreads();
     if (s_fail) break;
-    // ---- epilogue: warps w and w+4 share TMEM lanes 32(w%4).., columns split in halves ----
+    // ---- fold the exact group sums into this thread's double-float accumulators ----
     {
-      const int row = (warp & 3) * 32 + lane;
-      const int gr = r0 + row;
-      const uint32_t lane_base = uint32_t((warp & 3) * 32) << 16;
+      const float* sSA = sScale + buf * (TM + TN);
+      const float* sSB = sSA + TM;
       const float sa = sSA[row];
-#pragma unroll 1
+#pragma unroll
       for (int ch = 0; ch < 2; ++ch) {
-        const int col = (warp >> 2) * 32 + ch * 16;
-        float acc[kGroups][16];
+        const int col = colbase + ch * 16;
+        float gacc[kGroups][16];
 #pragma unroll
-        for (int g = 0; g < kGroups; ++g) tmem_ld16(tmem + lane_base + uint32_t(g * TN + col), acc[g]);
+        for (int g = 0; g < kGroups; ++g) tmem_ld16(tmem + lane_base + uint32_t(g * TN + col), gacc[g]);
         tmem_wait_ld();
-        if (gr < m) {
-          float* ph = Chi + int64_t(gr) * ldc;
-          float* pl = Clo + int64_t(gr) * ldc;
-#pragma unroll 4
-          for (int u = 0; u < 16; ++u) {
-            const int gc = c0 + col + u;
-            if (gc >= nc) break;
-            // s = sum_g acc_g 2^(-9g) as a double-float (acc_g are exact integers)
-            float h, l, e;
-            two_sum(acc[0][u], __fmul_rn(acc[1][u], 1.953125e-3f), h, l);
-            two_sum(h, __fmul_rn(acc[2][u], 3.814697265625e-06f), h, e);
-            l = __fadd_rn(l, e);
-            float w = 3.814697265625e-06f;
 #pragma unroll
-            for (int g = 3; g < kGroups; ++g) {
-              w = __fmul_rn(w, 1.953125e-3f);
-              l = __fadd_rn(l, __fmul_rn(acc[g][u], w));
-            }
-            fast_two_sum(h, l, h, l);
-            const float sc = __fmul_rn(sa, sSB[col + u]);
-            h = __fmul_rn(h, sc);
-            l = __fmul_rn(l, sc);
-            // C -= (h, l)
-            float s, t;
-            two_sum(ph[gc], -h, s, t);
-            t = __fadd_rn(t, __fsub_rn(pl[gc], l));
-            fast_two_sum(s, t, s, t);
-            ph[gc] = s;
-            pl[gc] = t;
+        for (int u = 0; u < 16; ++u) {
+          float h, l, e;
+          two_sum(gacc[0][u], __fmul_rn(gacc[1][u], 1.953125e-3f), h, l);
+          two_sum(h, __fmul_rn(gacc[2][u], 3.814697265625e-06f), h, e);
+          l = __fadd_rn(l, e);
+          float w = 3.814697265625e-06f;
+#pragma unroll
+          for (int g = 3; g < kGroups; ++g) {
+            w = __fmul_rn(w, 1.953125e-3f);
+            l = __fadd_rn(l, __fmul_rn(gacc[g][u], w));
           }
+          const float sc = __fmul_rn(sa, sSB[col + u]);
+          h = __fmul_rn(h, sc);
+          l = __fmul_rn(l, sc);
+          float s1, t1;
+          two_sum(acc_h[ch * 16 + u], h, s1, t1);
+          t1 = __fadd_rn(t1, __fadd_rn(acc_l[ch * 16 + u], l));
+          fast_two_sum(s1, t1, acc_h[ch * 16 + u], acc_l[ch * 16 + u]);
         }
       }
     }
     tc_fence_before();
     __syncthreads();
+  }
+  // ---- C -= accumulated product, once ----
+  if (!s_fail) {
+    const int gr = r0 + row;
+    if (gr < m) {
+      float* ph = Chi + int64_t(gr) * ldc + c0 + colbase;
+      float* pl = Clo + int64_t(gr) * ldc + c0 + colbase;
+      const bool vec_c = (((reinterpret_cast<uintptr_t>(ph) | reinterpret_cast<uintptr_t>(pl)) & 15) == 0) &&
+                         c0 + colbase + 31 < nc;
+      if (vec_c) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          float4 hv = reinterpret_cast<float4*>(ph)[q], lv = reinterpret_cast<float4*>(pl)[q];
+          float hh[4] = {hv.x, hv.y, hv.z, hv.w}, ll[4] = {lv.x, lv.y, lv.z, lv.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            float sx, tx;
+            two_sum(hh[u], -acc_h[q * 4 + u], sx, tx);
+            tx = __fadd_rn(tx, __fsub_rn(ll[u], acc_l[q * 4 + u]));
+            fast_two_sum(sx, tx, hh[u], ll[u]);
+          }
+          reinterpret_cast<float4*>(ph)[q] = make_float4(hh[0], hh[1], hh[2], hh[3]);
+          reinterpret_cast<float4*>(pl)[q] = make_float4(ll[0], ll[1], ll[2], ll[3]);
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+          if (c0 + colbase + u < nc) {
+            float sx, tx;
+            two_sum(ph[u], -acc_h[u], sx, tx);
+            tx = __fadd_rn(tx, __fsub_rn(pl[u], acc_l[u]));
+            fast_two_sum(sx, tx, ph[u], pl[u]);
+          }
+        }
+      }
+    }
   }
   if (s_fail && tid == 0) {
     status_error(st, UPDES_ERR_TIMEOUT);

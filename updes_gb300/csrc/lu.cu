@@ -11,6 +11,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -25,7 +27,7 @@ constexpr int kPanelThreads = 256;
 struct Cand {
   double absval;
   int idx;
-  int pad;
+  int tag;  // column index + 1 this candidate belongs to (written last)
 };
 
 // Cooperative panel factorisation of W[k:n, k:k+nb] (FP64), result to F.
@@ -38,10 +40,13 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
                                                               int32_t* __restrict__ piv, unsigned int* bar,
                                                               Cand* cand, double* cand_row, double* diag_row,
                                                               int32_t* swap_map, DeviceStatus* st) {
-  extern __shared__ double smem[];
-  double* tile = smem;                                   // rows_per_cta x nb
-  double* prow = tile + int64_t(rows_per_cta) * nb;      // nb
-  double* drow = prow + nb;                              // nb
+  // The FP64 path factors in FP64; the mixed path's panel reads the FP32 rounding (hi plane) of the
+  // double-float trailing matrix and works in FP32 (each update one rounding, like an FMA).
+  using TT = typename std::conditional<DF_IN, float, double>::type;
+  extern __shared__ __align__(16) unsigned char panel_smem[];
+  TT* tile = reinterpret_cast<TT*>(panel_smem);          // rows_per_cta x nb
+  TT* prow = tile + int64_t(rows_per_cta) * nb;          // nb
+  TT* drow = prow + nb;                                  // nb
   __shared__ double red_v[kPanelThreads / 32];
   __shared__ int red_i[kPanelThreads / 32];
   __shared__ int s_best_local, s_gw, s_p;
@@ -51,12 +56,13 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
   const int rbase = k + g * rows_per_cta;
   const int rcount = max(0, min(rows_per_cta, n - rbase));
 
-  for (int64_t e = tid; e < int64_t(rcount) * nb; e += blockDim.x) {
-    const int l = int(e / nb), c = int(e % nb);
-    const int64_t idx = int64_t(rbase + l) * ldw + k + c;
-    if constexpr (DF_IN) tile[e] = double(static_cast<const float*>(W)[idx]) + double(Wlo[idx]);
-    else tile[e] = static_cast<const double*>(W)[idx];
-  }
+  // rows over warps, columns over lanes (no division by the runtime panel width)
+  for (int l = wid; l < rcount; l += kPanelThreads / 32)
+    for (int c = lane; c < nb; c += 32) {
+      const int64_t idx = int64_t(rbase + l) * ldw + k + c;
+      if constexpr (DF_IN) tile[int64_t(l) * nb + c] = static_cast<const float*>(W)[idx];
+      else tile[int64_t(l) * nb + c] = static_cast<const double*>(W)[idx];
+    }
   __syncthreads();
 
   for (int j = 0; j < nb; ++j) {
@@ -68,7 +74,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
     for (int l = tid; l < rcount; l += blockDim.x) {
       const int gr = rbase + l;
       if (gr < diag) continue;
-      const double v = fabs(tile[int64_t(l) * nb + j]);
+      const double v = fabs(double(tile[int64_t(l) * nb + j]));
       const double vv = (v != v) ? INFINITY : v;  // NaN wins, so it surfaces as a bad pivot
       if (vv > bv || (vv == bv && gr < bi)) { bv = vv; bi = gr; }
     }
@@ -82,20 +88,44 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
     if (tid == 0) {
       for (int w = 1; w < kPanelThreads / 32; ++w)
         if (red_v[w] > bv || (red_v[w] == bv && red_i[w] < bi)) { bv = red_v[w]; bi = red_i[w]; }
-      Cand c;
-      c.absval = bv;
-      c.idx = bi;
-      c.pad = 0;
-      __stcg(reinterpret_cast<double2*>(cand + par * G + g), *reinterpret_cast<double2*>(&c));
       s_best_local = (bi == 0x7fffffff) ? -1 : bi - rbase;
+      red_v[0] = bv;
+      red_i[0] = bi;
     }
     __syncthreads();
     if (s_best_local >= 0)
       for (int c = tid; c < nb; c += blockDim.x)
-        __stcg(cand_row + (int64_t(par) * G + g) * nb + c, tile[int64_t(s_best_local) * nb + c]);
+        __stcg(cand_row + (int64_t(par) * G + g) * nb + c, double(tile[int64_t(s_best_local) * nb + c]));
     if (diag >= rbase && diag < rbase + rcount)
-      for (int c = tid; c < nb; c += blockDim.x) __stcg(diag_row + par * nb + c, tile[int64_t(diag - rbase) * nb + c]);
-    if (!grid_barrier(bar, G, st, 1)) return;
+      for (int c = tid; c < nb; c += blockDim.x)
+        __stcg(diag_row + par * nb + c, double(tile[int64_t(diag - rbase) * nb + c]));
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+      // publish: value, then (index, tag) as one 8-byte word after a fence
+      Cand* slot = cand + par * G + g;
+      __stcg(&slot->absval, red_v[0]);
+      __threadfence();
+      const unsigned long long it = (unsigned long long)(unsigned)red_i[0] |
+                                    ((unsigned long long)(unsigned)(diag + 1) << 32);
+      atomicExch(reinterpret_cast<unsigned long long*>(&slot->idx), it);
+    }
+    // wait until every CTA has published its candidate for this column (bounded)
+    for (int w = tid; w < G; w += blockDim.x) {
+      volatile unsigned long long* tw = reinterpret_cast<volatile unsigned long long*>(&(cand + par * G + w)->idx);
+      long long it = 0;
+      while (int((*tw) >> 32) != diag + 1) {
+        if (++it > kSpinLimit) {
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, 1);
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+    }
+    // one answer for the whole CTA (another CTA may set the status word at any moment)
+    if (__syncthreads_or(*reinterpret_cast<volatile int*>(&st->error) != 0)) return;
     // 2. global pivot
     bv = -1.0;
     bi = 0x7fffffff;
@@ -124,8 +154,8 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
     __syncthreads();
     const int gw = s_gw, p = s_p;
     for (int c = tid; c < nb; c += blockDim.x) {
-      prow[c] = __ldcg(cand_row + (int64_t(par) * G + gw) * nb + c);
-      drow[c] = __ldcg(diag_row + par * nb + c);
+      prow[c] = TT(__ldcg(cand_row + (int64_t(par) * G + gw) * nb + c));
+      drow[c] = TT(__ldcg(diag_row + par * nb + c));
     }
     __syncthreads();
     if (tid == 0) {
@@ -143,25 +173,23 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
     // 4. scale the column and update the rest of the panel
     const double pv = s_pivval;
     if (pv != 0.0 && isfinite(pv)) {
-      const double rinv = 1.0 / pv;
+      const TT rinv = TT(1.0 / pv);
       const int l0 = max(0, diag + 1 - rbase);
       for (int l = l0 + tid; l < rcount; l += blockDim.x) tile[int64_t(l) * nb + j] *= rinv;
       __syncthreads();
-      const int w = nb - j - 1;
-      if (w > 0) {
-        const int64_t tot = int64_t(rcount - l0) * w;
-        for (int64_t e = tid; e < tot; e += blockDim.x) {
-          const int l = l0 + int(e / w), c = j + 1 + int(e % w);
-          tile[int64_t(l) * nb + c] -= tile[int64_t(l) * nb + j] * prow[c];
+      if (j + 1 < nb) {
+        // rank-1 update of the panel's remaining columns: rows over warps, columns over lanes
+        for (int l = l0 + wid; l < rcount; l += kPanelThreads / 32) {
+          TT* row = tile + int64_t(l) * nb;
+          const TT a = row[j];
+          for (int c = j + 1 + lane; c < nb; c += 32) row[c] -= a * prow[c];
         }
       }
     }
     __syncthreads();
   }
-  for (int64_t e = tid; e < int64_t(rcount) * nb; e += blockDim.x) {
-    const int l = int(e / nb), c = int(e % nb);
-    F[int64_t(rbase + l) * ldf + k + c] = TF(tile[e]);
-  }
+  for (int l = wid; l < rcount; l += kPanelThreads / 32)
+    for (int c = lane; c < nb; c += 32) F[int64_t(rbase + l) * ldf + k + c] = TF(tile[int64_t(l) * nb + c]);
   if (swap_map && g == 0 && tid < 32) {
     // net permutation of the interchanges piv[k, k+nb): content tracking over <= 2 nb rows
     __shared__ int rows_s[128], cont_s[128];
@@ -220,26 +248,38 @@ __global__ void swap_scatter_kernel(SwapJobs jobs, int64_t ld, const int32_t* __
   jobs.plane[j][int64_t(map[1 + q]) * ld + c] = scratch[(int64_t(j) * 128 + q) * scratch_ld + (c - jobs.c0[j])];
 }
 
-// U = L^-1 W on rows [k, k+nb), columns [c0, c1): L unit lower from F (FP32), W double-float, FP64 arithmetic,
-// result rounded into F.
+// U = L^-1 W on rows [k, k+nb), columns [c0, c1): L unit lower from F (FP32), W double-float.  Each row is
+// w_i - sum_j L_ij x_j accumulated in double-float (exact FP32 products, compensated sums) and rounded once
+// to FP32 into F: FP32 ALU only.
 __global__ void __launch_bounds__(64) trsm_df_kernel(float* Whi, const float* Wlo, int64_t ld, int k, int nb,
                                                      int64_t c0, int64_t c1) {
-  __shared__ double sL[64 * 64];
+  __shared__ float sL[64][65];
+  __shared__ float sX[64][65];
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e / nb, j = e % nb;
-    sL[e] = (j < i) ? double(Whi[int64_t(k + i) * ld + k + j]) : 0.0;
+    sL[i][j] = (j < i) ? Whi[int64_t(k + i) * ld + k + j] : 0.f;
   }
   __syncthreads();
-  const int64_t c = c0 + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x;
+  const int64_t c = c0 + int64_t(blockIdx.x) * blockDim.x + t;
   if (c >= c1) return;
-  double x[64];
   for (int i = 0; i < nb; ++i) {
     const int64_t idx = int64_t(k + i) * ld + c;
-    double v = double(Whi[idx]) + double(Wlo[idx]);
-    for (int j = 0; j < i; ++j) v -= sL[i * nb + j] * x[j];
-    x[i] = v;
+    float sh = Whi[idx], sl = Wlo[idx];
+    for (int j = 0; j < i; ++j) {
+      const float f = -sL[i][j], xj = sX[j][t];
+      const float p = __fmul_rn(f, xj);
+      const float e = __fmaf_rn(f, xj, -p);
+      const float s2 = __fadd_rn(sh, p);
+      const float bb = __fsub_rn(s2, sh);
+      const float tt = __fadd_rn(__fsub_rn(sh, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
+      sh = s2;
+      sl = __fadd_rn(sl, __fadd_rn(tt, e));
+    }
+    const float xi = __fadd_rn(sh, sl);
+    sX[i][t] = xi;
+    Whi[idx] = xi;
   }
-  for (int i = 0; i < nb; ++i) Whi[int64_t(k + i) * ld + c] = float(x[i]);
 }
 
 // Apply the row interchanges piv[k0, k0+cnt) to columns [c0, c1) of M.
@@ -348,13 +388,15 @@ int launch_panel(void* W, const float* Wlo, int64_t ldw, TF* F, int64_t ldf, int
                  DeviceStatus* st, cudaStream_t s) {
   const int sms = num_sms();
   const int m = n - k;
-  int G = std::min(sms, int(ceil_div(m, 32)));
+  const size_t esz = DF_IN ? sizeof(float) : sizeof(double);
+  // fewer CTAs make each column's candidate exchange cheaper; the FP32 panel fits in 32 CTAs up to ~24k rows
+  int G = std::min(DF_IN ? 32 : sms, int(ceil_div(m, 32)));
   int rows = int(ceil_div(m, G));
-  size_t smem = (size_t(rows) * w + 2 * w) * sizeof(double);
+  size_t smem = (size_t(rows) * w + 2 * w) * esz;
   while (smem > 200 * 1024 && G < 2 * sms) {
     ++G;
     rows = int(ceil_div(m, G));
-    smem = (size_t(rows) * w + 2 * w) * sizeof(double);
+    smem = (size_t(rows) * w + 2 * w) * esz;
   }
   if (smem > 200 * 1024) return UPDES_ERR_UNSUPPORTED;
   auto kern = panel_kernel<TF, DF_IN>;
@@ -372,9 +414,15 @@ int launch_panel(void* W, const float* Wlo, int64_t ldw, TF* F, int64_t ldf, int
   return UPDES_OK;
 }
 
+constexpr int kOuterNb = 4 * kLuNb;  // 256: width of the big exact trailing updates
+
+size_t lu_df_swap_bytes(int n) { return (3ull * 128 * (size_t(n) + 64) * sizeof(float) + 255) & ~size_t(255); }
+
 size_t lu_df_workspace_bytes(int n) {
-  // panel scratch (rounded up to 256 B), 2 KB swap map, 3 x 128 rows of swap scratch
-  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + 2048 + 3ull * 128 * (size_t(n) + 64) * sizeof(float);
+  // panel scratch (rounded up to 256 B), 2 KB swap map, 3 x 128 rows of swap scratch, digit scratch of the
+  // tensor-core update
+  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + 2048 + lu_df_swap_bytes(n) +
+         ozaki3_scratch_bytes(n, n, kOuterNb);
 }
 
 int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* ws, size_t ws_bytes, DeviceStatus* st,
@@ -390,8 +438,15 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   int32_t* swap_map = reinterpret_cast<int32_t*>(after);
   float* scratch = reinterpret_cast<float*>(after + 2048);
   const int64_t scratch_ld = int64_t(n) + 64;
-  UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256, s));
-  constexpr int kOuter = 4 * kLuNb;  // 256: width of the exact trailing updates
+  void* digits = after + 2048 + lu_df_swap_bytes(n);
+  const size_t digits_bytes = ozaki3_scratch_bytes(n, n, kOuterNb);
+  // UPDES_OZAKI=3 selects the persistent TMA-fed update (gemm_tc3.cu) instead of gemm_tc.cu's
+  static const bool use_v2 = [] {
+    const char* v = std::getenv("UPDES_OZAKI");
+    return !(v && v[0] == '3');
+  }();
+  UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256 + 2 * 1024 * sizeof(Cand), s));  // barrier words and candidate tags
+  constexpr int kOuter = kOuterNb;
   auto swaps = [&](int k, int w) -> int {
     SwapJobs j{};
     int nj = 0;
@@ -424,6 +479,10 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   };
   auto upd = [&](int r0, int r1, int c0, int c1, int kk0, int kk1) -> int {
     // W[r0:r1, c0:c1] -= F[r0:r1, kk0:kk1] * F[kk0:kk1, c0:c1]
+    if (!use_v2)
+      return ozaki3_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld, Whi + int64_t(r0) * ld + kk0,
+                           ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0, c1 - c0, kk1 - kk0, digits, digits_bytes, st,
+                           s);
     return ozaki_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld, Whi + int64_t(r0) * ld + kk0,
                         ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0, c1 - c0, kk1 - kk0, st, s);
   };
@@ -463,7 +522,7 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
   Cand* cand = reinterpret_cast<Cand*>(base + 256);
   double* cand_row = reinterpret_cast<double*>(base + 256 + 2 * 1024 * sizeof(Cand));
   double* diag_row = cand_row + 2ll * 1024 * nb;
-  UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256, s));
+  UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256 + 2 * 1024 * sizeof(Cand), s));  // barrier words and candidate tags
   for (int k = 0; k < n; k += nb) {
     const int w = std::min(nb, n - k);
     {
@@ -523,20 +582,35 @@ __device__ __forceinline__ void df_fma(float f, float xh, float xl, float& sh, f
   const float e = __fmaf_rn(f, xh, -p);  // exact error of the product
   const float s = __fadd_rn(sh, p);
   const float bb = __fsub_rn(s, sh);
-  const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-  sh = s;
-  sl = __fadd_rn(sl, __fadd_rn(t, __fmaf_rn(f, xl, e)));
+  float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  t = __fadd_rn(t, __fadd_rn(sl, __fmaf_rn(f, xl, e)));
+  sh = __fadd_rn(s, t);  // renormalised after every term
+  sl = __fsub_rn(t, __fsub_rn(sh, s));
+}
+
+// (qh, ql) = (bh + bl) / d for an FP32 divisor d
+__device__ __forceinline__ void df_div1(float bh, float bl, float d, float& qh, float& ql) {
+  const float q1 = __fdiv_rn(bh, d);
+  const float p = __fmul_rn(q1, d);
+  const float pe = __fmaf_rn(q1, d, -p);  // q1 * d = p + pe exactly
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(bh, p), pe), bl);
+  const float q2 = __fdiv_rn(r, d);
+  qh = __fadd_rn(q1, q2);
+  ql = __fsub_rn(q2, __fsub_rn(qh, q1));
 }
 
 template <typename TF, int MODE>
 __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int64_t ldf, int n, double* x,
-                                                   int* ticket, int* flags, DeviceStatus* st) {
+                                                   int* ticket, int* flags, DeviceStatus* st,
+                                                   const float* __restrict__ dinv) {
   extern __shared__ __align__(16) unsigned char trsv_smem[];
   TF(*sT)[kTB + 1] = reinterpret_cast<TF(*)[kTB + 1]>(trsv_smem);
   double* sxd = reinterpret_cast<double*>(trsv_smem + sizeof(TF) * kTB * (kTB + 1));  // 64
   float* sxh = reinterpret_cast<float*>(sxd + kTB);                                    // 64
   float* sxl = sxh + kTB;                                                              // 64
   double* sacc = reinterpret_cast<double*>(sxl + kTB);                                 // 64
+  float(*sDl)[kTB + 1] = reinterpret_cast<float(*)[kTB + 1]>(sacc + kTB);              // 64 x 65 (dinv only)
+  float(*sDh)[kTB + 1] = sDl + kTB;                                                    // 64 x 65 (dinv only)
   __shared__ int s_blk;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = int(ceil_div(n, kTB));
@@ -549,6 +623,23 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
   const int blk = fwd ? t : nblk - 1 - t;
   const int r0 = blk * kTB;
   const int rows = min(kTB, n - r0);
+  // inputs that no other block writes, fetched before any wait: this block's right-hand side and, with
+  // dinv, its inverted diagonal block (modes 2 and 3 use the transposes of the U and L inverses)
+  const double b_own = (tid < rows) ? x[r0 + tid] : 0.0;
+  if constexpr (sizeof(TF) == 4) {
+    if (dinv) {
+      constexpr int which = (MODE == 0 || MODE == 3) ? 0 : 1;  // 0: inv(L_bb), 1: inv(U_bb)
+      constexpr bool tr = (MODE >= 2);
+      const float* Dh = dinv + (size_t(blk) * 4 + which * 2) * kTB * kTB;
+      const float* Dlo = Dh + kTB * kTB;
+      for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+        const int a = e >> 6, b = e & 63;
+        const int ra = tr ? b : a, cb = tr ? a : b;
+        sDh[ra][cb] = __ldg(Dh + e);
+        sDl[ra][cb] = __ldg(Dlo + e);
+      }
+    }
+  }
 
   auto load_tile = [&](int c0, TF (&pre)[16]) {
 #pragma unroll
@@ -581,22 +672,29 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
   for (int i = 0; i < 8; ++i) { ah[i] = 0.f; al[i] = 0.f; ad[i] = 0.0; }
   TF pre[16];
   if (t > 0) load_tile((fwd ? 0 : nblk - 1) * kTB, pre);
+  // Blocks finish in ticket order (each waits for all earlier ones), so flags[nblk] counts finished
+  // blocks: a CTA re-reads it only when it needs a block beyond the last count it saw.
+  __shared__ int s_done;
+  if (tid == 0) s_done = 0;
   for (int q = 0; q < t; ++q) {
     const int jb = fwd ? q : nblk - 1 - q;
     const int c0 = jb * kTB;
     const int cols = min(kTB, n - c0);
-    if (tid == 0) {
-      volatile int* vf = flags + jb;
+    if (tid == 0 && s_done <= q) {
+      volatile int* vc = flags + nblk;
       long long it = 0;
-      while (*vf == 0) {
+      int d;
+      while ((d = *vc) <= q) {
         if (++it > kSpinLimit) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 10 + MODE);
+          d = q + 1;
           break;
         }
-        __nanosleep(32);
+        __nanosleep(20);
       }
       __threadfence();
+      s_done = d;
     }
     __syncthreads();
     store_tile(pre);
@@ -628,6 +726,48 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) sacc[warp * 8 + i] = v;
   }
+  if constexpr (sizeof(TF) == 4) {
+    if (dinv) {
+      // x_blk = D (b - off-diagonal part), D the inverted diagonal block (double-float planes, prefetched):
+      // a matvec, no dependent chain
+      __syncthreads();
+      if (tid < kTB) {
+        const double v = tid < rows ? b_own - sacc[tid] : 0.0;
+        const float hh = float(v);
+        sxh[tid] = hh;
+        sxl[tid] = float(v - double(hh));
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int rr = warp * 8 + i;
+        float ph = 0.f, pl = 0.f;
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int cc = lane + 32 * hh;
+          const float dh = sDh[rr][cc], dl = sDl[rr][cc];
+          // (ph, pl) += (dh + dl)(xh + xl), dropping dl * xl
+          const float p = __fmul_rn(dh, sxh[cc]);
+          const float pe = __fmaf_rn(dh, sxh[cc], -p);
+          const float s0 = __fadd_rn(ph, p);
+          const float bb = __fsub_rn(s0, ph);
+          float t = __fadd_rn(__fsub_rn(ph, __fsub_rn(s0, bb)), __fsub_rn(p, bb));
+          t = __fadd_rn(t, __fadd_rn(pl, __fmaf_rn(dh, sxl[cc], __fmaf_rn(dl, sxh[cc], pe))));
+          ph = __fadd_rn(s0, t);
+          pl = __fsub_rn(t, __fsub_rn(ph, s0));
+        }
+        double v = double(ph) + double(pl);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0 && rr < rows) x[r0 + rr] = v;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        atomicAdd(flags + nblk, 1);  // blocks finish in order: this is block number t
+      }
+      return;
+    }
+  }
   // diagonal block
   {
     TF dpre[16];
@@ -635,49 +775,167 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
     store_tile(dpre);
   }
   __syncthreads();
-  if (tid < 32) {
-    double xi_lane[2] = {0.0, 0.0};
+  __shared__ double s_rdiag[kTB];
+  constexpr bool unit = (MODE == 0 || MODE == 3);
+  if (sizeof(TF) == 8 && !unit && tid < rows) s_rdiag[tid] = 1.0 / double(sT[tid][tid]);
+  __syncthreads();
+  if (sizeof(TF) == 4 && tid < 32) {
+    // FP32 factors: the same column-oriented substitution in double-float arithmetic on the FP32 pipes
+    // (one warp's FP64 instructions would serialise on the SM's few FP64 units)
+    float v0h = 0.f, v0l = 0.f, v1h = 0.f, v1l = 0.f;
+    if (tid < rows) {
+      const double v = x[r0 + tid] - sacc[tid];
+      v0h = float(v);
+      v0l = float(v - double(v0h));
+    }
+    if (tid + 32 < rows) {
+      const double v = x[r0 + tid + 32] - sacc[tid + 32];
+      v1h = float(v);
+      v1l = float(v - double(v1h));
+    }
     for (int s2 = 0; s2 < rows; ++s2) {
       const int i = fwd ? s2 : rows - 1 - s2;
-      double part_sum = 0.0;
-      for (int j = tid; j < rows; j += 32) {
-        const bool dep = fwd ? (j < i) : (j > i);
-        if (dep) part_sum += double(sT[i][j]) * xi_lane[j >> 5];
+      const bool hi_slot = (i >> 5) != 0;
+      float xh = __shfl_sync(0xffffffffu, hi_slot ? v1h : v0h, i & 31);
+      float xl = __shfl_sync(0xffffffffu, hi_slot ? v1l : v0l, i & 31);
+      if (!unit) df_div1(xh, xl, float(sT[i][i]), xh, xl);
+      if ((i & 31) == tid) {
+        if (hi_slot) { v1h = xh; v1l = xl; }
+        else { v0h = xh; v0l = xl; }
       }
-      for (int o = 16; o > 0; o >>= 1) part_sum += __shfl_xor_sync(0xffffffffu, part_sum, o);
-      double v = x[r0 + i] - sacc[i] - part_sum;
-      constexpr bool unit = (MODE == 0 || MODE == 3);
-      if (!unit) v = v / double(sT[i][i]);
-      if ((i & 31) == tid) xi_lane[i >> 5] = v;
+      const int ra = tid, rb = tid + 32;
+      if (fwd ? ra > i : ra < i) df_fma(-float(sT[ra][i]), xh, xl, v0h, v0l);
+      if (rb < rows && (fwd ? rb > i : rb < i)) df_fma(-float(sT[rb][i]), xh, xl, v1h, v1l);
     }
-    for (int i = tid; i < rows; i += 32) x[r0 + i] = xi_lane[i >> 5];
+    if (tid < rows) x[r0 + tid] = double(v0h) + double(v0l);
+    if (tid + 32 < rows) x[r0 + tid + 32] = double(v1h) + double(v1l);
+  } else if (sizeof(TF) == 8 && tid < 32) {
+    // column-oriented substitution: lane owns rows lane and lane+32; x_i is broadcast by one shuffle and
+    // every unsolved row is updated right away (no global loads on the dependent chain)
+    double v0 = 0.0, v1 = 0.0;
+    if (tid < rows) v0 = x[r0 + tid] - sacc[tid];
+    if (tid + 32 < rows) v1 = x[r0 + tid + 32] - sacc[tid + 32];
+    for (int s2 = 0; s2 < rows; ++s2) {
+      const int i = fwd ? s2 : rows - 1 - s2;
+      double xi = __shfl_sync(0xffffffffu, (i >> 5) ? v1 : v0, i & 31);
+      if (!unit) xi *= s_rdiag[i];
+      if ((i & 31) == tid) {
+        if (i >> 5) v1 = xi;
+        else v0 = xi;
+      }
+      const int ra = tid, rb = tid + 32;
+      if (fwd ? ra > i : ra < i) v0 -= double(sT[ra][i]) * xi;
+      if (rb < rows && (fwd ? rb > i : rb < i)) v1 -= double(sT[rb][i]) * xi;
+    }
+    if (tid < rows) x[r0 + tid] = v0;
+    if (tid + 32 < rows) x[r0 + tid + 32] = v1;
   }
   __syncthreads();
   if (tid == 0) {
     __threadfence();
-    atomicExch(flags + blk, 1);
+    atomicAdd(flags + nblk, 1);  // blocks finish in order: this is block number t
   }
 }
 
 }  // namespace
 
 template <typename TF>
-int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s) {
+int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
+              const float* dinv) {
   const int nblk = int(ceil_div(n, kTB));
   StatScope sc(kStatTrsv, s, double(n) * n, double(n) * n * 0.5 * sizeof(TF));
-  UPDES_CUDA_TRY(cudaMemsetAsync(sync_ws, 0, sizeof(int) * (nblk + 1), s));
+  UPDES_CUDA_TRY(cudaMemsetAsync(sync_ws, 0, sizeof(int) * (nblk + 2), s));
   int* ticket = sync_ws;
   int* flags = sync_ws + 1;
-  const size_t smem = sizeof(TF) * kTB * (kTB + 1) + kTB * (8 + 4 + 4 + 8);
+  if (sizeof(TF) != 4) dinv = nullptr;
+  const size_t smem =
+      sizeof(TF) * kTB * (kTB + 1) + kTB * (8 + 4 + 4 + 8) + (dinv ? 2 * sizeof(float) * kTB * (kTB + 1) : 0);
+  static bool attr = false;
+  if (!attr) {
+    const int big = int(sizeof(TF) * kTB * (kTB + 1) + kTB * 24 + 2 * sizeof(float) * kTB * (kTB + 1));
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    attr = true;
+  }
   switch (mode) {
-    case 0: trsv_kernel<TF, 0><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st); break;
-    case 1: trsv_kernel<TF, 1><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st); break;
-    case 2: trsv_kernel<TF, 2><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st); break;
-    default: trsv_kernel<TF, 3><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st); break;
+    case 0: trsv_kernel<TF, 0><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st, dinv); break;
+    case 1: trsv_kernel<TF, 1><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st, dinv); break;
+    case 2: trsv_kernel<TF, 2><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st, dinv); break;
+    default: trsv_kernel<TF, 3><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st, dinv); break;
   }
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }
 
-template int trsv_impl<double>(int, const double*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t);
-template int trsv_impl<float>(int, const float*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t);
+template int trsv_impl<double>(int, const double*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
+                               const float*);
+template int trsv_impl<float>(int, const float*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
+                              const float*);
+
+namespace {
+
+// Inverses of the 64 x 64 diagonal blocks of FP32 factors (unit lower L_bb and upper U_bb), formed in FP64
+// and stored as double-float planes: dinv[blk] = {inv(L) hi, inv(L) lo, inv(U) hi, inv(U) lo}, each 64 x 64
+// row-major.  Rows past n (last block) are completed by the identity.  Threads 0-63 form the columns of
+// inv(L), threads 64-127 those of inv(U), each by substitution against a unit vector.
+__global__ void __launch_bounds__(128) diag_inverse_kernel(const float* __restrict__ F, int64_t ldf, int n,
+                                                           float* __restrict__ dinv) {
+  extern __shared__ double di_smem[];
+  double(*B)[kTB + 1] = reinterpret_cast<double(*)[kTB + 1]>(di_smem);          // the diagonal block
+  double(*X)[kTB + 1] = reinterpret_cast<double(*)[kTB + 1]>(di_smem + kTB * (kTB + 1));      // inv(L)
+  double(*Y)[kTB + 1] = reinterpret_cast<double(*)[kTB + 1]>(di_smem + 2 * kTB * (kTB + 1));  // inv(U)
+  const int blk = blockIdx.x, r0 = blk * kTB, rows = min(kTB, n - r0);
+  for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+    const int i = e >> 6, j = e & 63;
+    double v = (i == j) ? 1.0 : 0.0;
+    if (i < rows && j < rows) v = double(F[int64_t(r0 + i) * ldf + r0 + j]);
+    B[i][j] = v;
+  }
+  __syncthreads();
+  const int j = threadIdx.x & 63;
+  if (threadIdx.x < 64) {
+    // L X = I: column j, forward (unit diagonal)
+    for (int i = 0; i < kTB; ++i) {
+      double v = (i == j) ? 1.0 : 0.0;
+      for (int k = j; k < i; ++k) v -= B[i][k] * X[k][j];
+      X[i][j] = (i < j) ? 0.0 : v;
+    }
+  } else {
+    // U Y = I: column j, backward
+    for (int i = kTB - 1; i >= 0; --i) {
+      double v = (i == j) ? 1.0 : 0.0;
+      for (int k = i + 1; k <= j; ++k) v -= B[i][k] * Y[k][j];
+      Y[i][j] = (i > j) ? 0.0 : v / B[i][i];
+    }
+  }
+  __syncthreads();
+  float* out = dinv + size_t(blk) * 4 * kTB * kTB;
+  for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+    const int i = e >> 6, c = e & 63;
+    const double l = X[i][c], u = Y[i][c];
+    const float lh = float(l), uh = float(u);
+    out[e] = lh;
+    out[kTB * kTB + e] = float(l - double(lh));
+    out[2 * kTB * kTB + e] = uh;
+    out[3 * kTB * kTB + e] = float(u - double(uh));
+  }
+}
+
+}  // namespace
+
+size_t diag_inverse_bytes(int n) { return size_t(ceil_div(n, kTB)) * 4 * kTB * kTB * sizeof(float); }
+
+int diag_inverse(int n, const float* F, int64_t ldf, float* dinv, cudaStream_t s) {
+  const size_t smem = 3 * kTB * (kTB + 1) * sizeof(double);
+  static bool attr = false;
+  if (!attr) {
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    attr = true;
+  }
+  StatScope sc(kStatOther, s, 2.0 * kTB * kTB * kTB / 3.0 * ceil_div(n, kTB), diag_inverse_bytes(n));
+  diag_inverse_kernel<<<unsigned(ceil_div(n, kTB)), 128, smem, s>>>(F, ldf, n, dinv);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}

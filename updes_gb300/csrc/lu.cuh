@@ -18,8 +18,15 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
                    DeviceStatus* st, cudaStream_t s, const LuHooks* hooks);
 
 // mode: 0 = L, 1 = U, 2 = U^T, 3 = L^T (x overwritten in place); sync_ws: ceil(n/64)+1 ints.
+// dinv (FP32 factors only, may be null): inverted diagonal blocks from diag_inverse, applied as matvecs
+// instead of the substitution inside each block.
 template <typename TF>
-int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s);
+int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
+              const float* dinv = nullptr);
+
+// Inverses of the 64 x 64 diagonal blocks of FP32 LU factors, as double-float planes (diag_inverse_bytes).
+size_t diag_inverse_bytes(int n);
+int diag_inverse(int n, const float* F, int64_t ldf, float* dinv, cudaStream_t s);
 
 // Mixed LU on a double-float working matrix (Whi, Wlo FP32 planes): factors in FP32 (overwriting Whi),
 // every trailing update formed exactly on the tensor cores and accumulated in double-float.

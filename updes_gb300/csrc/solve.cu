@@ -3,8 +3,10 @@
 // updes_solve replaces pde_solver's assemble_B -> lineax QR ->
 // core_compute_coefficients sequence (updes/operators.py:602-618) by one
 // factorisation of the augmented Kansa matrix K and refinement in FP64.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -76,13 +78,6 @@ __global__ void col_scale_kernel(const double* __restrict__ K, int64_t ld, int n
   dc[j] = ldexp(1.0, -e);
 }
 
-__global__ void scale_copy_kernel(const double* __restrict__ K, int64_t ldk, double* __restrict__ W, int64_t ldw,
-                                  int n, const double* __restrict__ dr, const double* __restrict__ dc) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t i = e / ldw, j = e % ldw;
-  if (i >= n) return;
-  W[i * ldw + j] = (j < n) ? dr[i] * K[i * ldk + j] * dc[j] : 0.0;
-}
 
 // out_i = dr_i * (bsign * b_i + ksign * sum_j K_ij dc_j x_j), one warp per row (dr, dc, b may be null)
 // With absout != null also writes absout_i = dr_i * (sum_j |K_ij dc_j x_j| + |b_i|) (backward-error denominators).
@@ -162,8 +157,103 @@ __global__ void __launch_bounds__(256) gemv_t_kernel(const double* __restrict__ 
   }
 }
 
+// Double-float matrix-vector products with the equilibrated K stored as FP32 planes (hi, lo):
+// exact FP32 products (FMA), compensated sums; the absolute sums for the backward error in FP32.
+__device__ __forceinline__ void df_acc(float kh, float kl, float a, float b, float& sh, float& sl, float& sa) {
+  const float p = __fmul_rn(kh, a);
+  const float e = __fmaf_rn(kh, a, -p);
+  const float s = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(s, sh);
+  float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  t = __fadd_rn(t, __fadd_rn(sl, __fmaf_rn(kh, b, __fmaf_rn(kl, a, e))));
+  sh = __fadd_rn(s, t);  // renormalise, so the low word never carries more than half an ulp of sh
+  sl = __fsub_rn(t, __fsub_rn(sh, s));
+  sa = __fadd_rn(sa, fabsf(p));
+}
+
+// out_i = ksign * sum_j K_ij x_j (x as FP32 planes xh, xl padded with zeros to ld); absout_i = sum |K_ij x_j|
+__global__ void __launch_bounds__(256) gemv_df_kernel(const float* __restrict__ Khi, const float* __restrict__ Klo,
+                                                      int64_t ld, int n, const float* __restrict__ xh,
+                                                      const float* __restrict__ xl, double ksign,
+                                                      double* __restrict__ out, double* __restrict__ absout) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float4* kh4 = reinterpret_cast<const float4*>(Khi + int64_t(row) * ld);
+  const float4* kl4 = reinterpret_cast<const float4*>(Klo + int64_t(row) * ld);
+  const float4* a4 = reinterpret_cast<const float4*>(xh);
+  const float4* b4 = reinterpret_cast<const float4*>(xl);
+  float sh = 0.f, sl = 0.f, sa = 0.f;
+  for (int64_t q = lane; q < ld / 4; q += 32) {
+    const float4 kh = kh4[q], kl = kl4[q], a = a4[q], b = b4[q];
+    df_acc(kh.x, kl.x, a.x, b.x, sh, sl, sa);
+    df_acc(kh.y, kl.y, a.y, b.y, sh, sl, sa);
+    df_acc(kh.z, kl.z, a.z, b.z, sh, sl, sa);
+    df_acc(kh.w, kl.w, a.w, b.w, sh, sl, sa);
+  }
+  double v = double(sh) + double(sl);
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+    sa += __shfl_xor_sync(0xffffffffu, sa, o);
+  }
+  if (lane == 0) {
+    out[row] = ksign * v;
+    if (absout) absout[row] = double(sa);
+  }
+}
+
+// out_j = ksign * sum_i K_ij x_i (transposed), 32 columns per CTA, 8 warps over the rows
+__global__ void __launch_bounds__(256) gemv_t_df_kernel(const float* __restrict__ Khi, const float* __restrict__ Klo,
+                                                        int64_t ld, int n, const float* __restrict__ xh,
+                                                        const float* __restrict__ xl, double ksign,
+                                                        double* __restrict__ out, double* __restrict__ absout) {
+  __shared__ double part[8][33];
+  __shared__ float apart[8][33];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  float sh = 0.f, sl = 0.f, sa = 0.f;
+  if (j < n)
+    for (int i = w; i < n; i += 8) {
+      const int64_t idx = int64_t(i) * ld + j;
+      df_acc(Khi[idx], Klo[idx], xh[i], xl[i], sh, sl, sa);
+    }
+  part[w][lane] = double(sh) + double(sl);
+  apart[w][lane] = sa;
+  __syncthreads();
+  if (w == 0 && j < n) {
+    double t = 0.0;
+    float ta = 0.f;
+    for (int q = 0; q < 8; ++q) {
+      t += part[q][lane];
+      ta += apart[q][lane];
+    }
+    out[j] = ksign * t;
+    if (absout) absout[j] = double(ta);
+  }
+}
+
+// (xh, xl) = FP32 planes of x (n values, zero padded to ld)
+__global__ void split_vec_kernel(const double* __restrict__ x, int n, int64_t ld, float* __restrict__ xh,
+                                 float* __restrict__ xl) {
+  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= ld) return;
+  const double v = j < n ? x[j] : 0.0;
+  const float h = float(v);
+  xh[j] = h;
+  xl[j] = float(v - double(h));
+}
+
+// W = double(hi) + double(lo): the FP64 working matrix from the double-float planes
+__global__ void join_df_kernel(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ W,
+                               int64_t total) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < total) W[e] = double(hi[e]) + double(lo[e]);
+}
+
 constexpr int kDotBlocks = 120;
-constexpr double kBwdFloor = 64.0 * 1.1102230246251565e-16;  // 64 unit roundoffs of FP64
+// Refinement stops at a componentwise backward error of 256 FP64 unit roundoffs: the residual is formed
+// from the double-float planes of K (48 significant bits per entry), which by themselves put the
+// measured backward error of an FP64 LU solution at roughly 50-100 unit roundoffs.
+constexpr double kBwdFloor = 256.0 * 1.1102230246251565e-16;
 
 // partial[b * nv + i] = sum over block b's chunk of V_i . w
 __global__ void __launch_bounds__(256) multi_dot_kernel(const double* __restrict__ V, int64_t ldv, int nv,
@@ -372,22 +462,22 @@ int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t l
 // x (contiguous, n) <- A^-1 x or A^-T x using the permutation in piv[n, 2n)
 template <typename TF>
 int solve_core(int n, const TF* F, int64_t ldf, const int32_t* piv, double* x, int trans, const LuWs& w,
-               cudaStream_t s) {
+               cudaStream_t s, const float* dinv = nullptr) {
   const int32_t* perm = piv + n;
   const unsigned g = unsigned(ceil_div(n, 256));
   if (!trans) {
     permute_kernel<<<g, 256, 0, s>>>(w.tmp, x, 1, 1, perm, n, 0);
     UPDES_LAUNCH_CHECK();
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv);
     if (e) return e;
     UPDES_CUDA_TRY(cudaMemcpyAsync(x, w.tmp, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
   } else {
     UPDES_CUDA_TRY(cudaMemcpyAsync(w.tmp, x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv);
     if (e) return e;
     permute_kernel<<<g, 256, 0, s>>>(x, w.tmp, 1, 1, perm, n, 1);
     UPDES_LAUNCH_CHECK();
@@ -475,9 +565,12 @@ namespace {
 
 struct SolveWs {
   LuWs lu;
-  double *K64, *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *partial, *h;
+  double *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *partial, *h;
+  float *Khi, *Klo;  // equilibrated K as double-float planes (kept for the refinement's residuals)
+  float *xh, *xl;    // FP32 planes of the vector a GEMV multiplies
   float* F32;  // hi plane = FP32 factors
   float* Wlo;
+  float* dinv;  // inverted 64 x 64 diagonal blocks of the FP32 factors (double-float planes)
   int32_t* piv;
   int32_t* state;  // [0] n of the factored system, [1] precision of its factors, [2] 1 when valid
   int64_t ld;
@@ -491,12 +584,16 @@ size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* ou
   char* lubase = c.take<char>(lub);
   if (base) lu_ws_layout(n, o.precision, lubase, &w.lu, false);
   w.ld = ld;
-  w.K64 = c.take<double>(size_t(n) * ld);
+  w.Khi = c.take<float>(2 * size_t(n) * ld);
+  w.Klo = w.Khi + size_t(n) * ld;
+  w.xh = c.take<float>(ld);
+  w.xl = c.take<float>(ld);
   w.W = c.take<double>(size_t(n) * ld);  // FP64 working matrix, or the hi and lo FP32 planes
   w.F32 = reinterpret_cast<float*>(w.W);
   w.Wlo = w.F32 + size_t(n) * ld;
   w.piv = c.take<int32_t>(2 * size_t(n));
   w.state = c.take<int32_t>(64);
+  w.dinv = c.take<float>(diag_inverse_bytes(n) / sizeof(float));
   w.dr = c.take<double>(n);
   w.dc = c.take<double>(n);
   w.bs = c.take<double>(n);
@@ -574,29 +671,30 @@ struct Timer {
 
 // Ks z = dr .* (K (dc .* z))
 // (trans: Ks^T z = dc .* (K^T (dr .* z)))
-int apply_K(const SolveWs& w, int n, const double* z, double* out, cudaStream_t s, bool trans = false) {
-  StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * n);
+int gemv_scaled(const SolveWs& w, int n, const double* z, double ksign, double* out, double* absout,
+                cudaStream_t s, bool trans) {
+  StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * double(w.ld));
+  split_vec_kernel<<<unsigned(ceil_div(w.ld, 256)), 256, 0, s>>>(z, n, w.ld, w.xh, w.xl);
+  UPDES_LAUNCH_CHECK();
   if (trans)
-    gemv_t_kernel<<<unsigned(ceil_div(n, 32)), 256, 0, s>>>(w.K64, w.ld, n, z, nullptr, w.dr, w.dc, 0.0, 1.0, out);
+    gemv_t_df_kernel<<<unsigned(ceil_div(n, 32)), 256, 0, s>>>(w.Khi, w.Klo, w.ld, n, w.xh, w.xl, ksign, out, absout);
   else
-    gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, z, nullptr, w.dr, w.dc,
-                                                                           0.0, 1.0, out);
+    gemv_df_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.Khi, w.Klo, w.ld, n, w.xh, w.xl, ksign,
+                                                                              out, absout);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
+}
+
+int apply_K(const SolveWs& w, int n, const double* z, double* out, cudaStream_t s, bool trans = false) {
+  return gemv_scaled(w, n, z, 1.0, out, nullptr, s, trans);
 }
 
 // out = bs - Ks x; also returns (on the host) the componentwise backward error
 // max_i |out_i| / (|Ks| |x| + |bs|)_i.
 int residual_scaled(const SolveWs& w, int n, const double* x, double* out, double* bwd, cudaStream_t s,
                     bool trans = false) {
-  StatScope sc(kStatGemv, s, 2.0 * n * n, 8.0 * n * n);
-  if (trans)
-    gemv_t_kernel<<<unsigned(ceil_div(n, 32)), 256, 0, s>>>(w.K64, w.ld, n, x, nullptr, w.dr, w.dc, 0.0, -1.0, out,
-                                                             w.absr);
-  else
-    gemv_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, x, nullptr, w.dr, w.dc,
-                                                                           0.0, -1.0, out, w.absr);
-  UPDES_LAUNCH_CHECK();
+  int e0 = gemv_scaled(w, n, x, -1.0, out, w.absr, s, trans);
+  if (e0) return e0;
   axpby_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(out, 1.0, w.bs, 1.0, n, nullptr);
   UPDES_LAUNCH_CHECK();
   axpby_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(w.absr, 1.0, w.bsabs, 1.0, n, nullptr);
@@ -614,13 +712,22 @@ int residual_scaled(const SolveWs& w, int n, const double* x, double* out, doubl
 
 int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s, bool trans = false) {
   if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
-  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
+  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv);
 }
 
 [[maybe_unused]] double host_norm(const std::vector<double>& v) {
   double s = 0;
   for (double a : v) s += a * a;
   return std::sqrt(s);
+}
+
+// UPDES_TRACE=1 in the environment prints the refinement history to stderr.
+bool trace_on() {
+  static const bool on = [] {
+    const char* v = std::getenv("UPDES_TRACE");
+    return v && v[0] == '1';
+  }();
+  return on;
 }
 
 // Restarted, right-preconditioned GMRES on Ks x = bs starting from w.x.
@@ -643,6 +750,9 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
     const double beta = std::sqrt(beta2);
     info->rel_residual = bnorm > 0 ? beta / bnorm : beta;
     info->backward_error = bwd;
+    if (trace_on())
+      std::fprintf(stderr, "[updes gmres n=%d prec=%d trans=%d] iters=%d rel_residual=%.3e backward_error=%.3e\n", n,
+                   precision, int(trans), total, info->rel_residual, bwd);
     if (!(beta == beta)) return UPDES_ERR_NOT_CONVERGED;
     if (beta <= o.tol * bnorm || bwd <= kBwdFloor) {
       info->converged = 1;
@@ -650,7 +760,9 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
     }
     if (total >= o.max_iters) break;
     if (beta > 0.5 * last_beta) {
-      if (++stalls >= 2) break;
+      if (++stalls >= 2) break;  // two restart cycles in a row without halving the residual
+    } else {
+      stalls = 0;
     }
     last_beta = beta;
     // V0 = r / beta
@@ -695,6 +807,8 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
       gv[j + 1] = -sn[j] * gv[j];
       gv[j] = cs[j] * gv[j];
       for (int i = 0; i <= j; ++i) H[size_t(i) * m + j] = hcol[i];
+      if (trace_on())
+        std::fprintf(stderr, "[updes gmres]   j=%d estimate=%.3e h_next=%.3e\n", j, std::fabs(gv[j + 1]) / bnorm, hn);
       if (std::fabs(gv[j + 1]) <= o.tol * bnorm || hn == 0.0) {
         ++j;
         ++total;
@@ -735,19 +849,21 @@ extern "C" int updes_solve_workspace(const updes_problem* p, const updes_solve_o
 
 namespace {
 
-// Equilibrated copy of K64 -> factors at `precision`; records the factored state in the workspace.
+// Factors of the equilibrated K (double-float planes) at `precision`; records the factored state.
 int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info, cudaStream_t s) {
   Timer t(s);
   int e;
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.state, 0, 4 * sizeof(int32_t), s));  // invalid until the factors are complete
+  const int64_t total = int64_t(n) * w.ld;
   if (precision == UPDES_PREC_FP64) {
-    scale_copy_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.K64, w.ld, w.W, w.ld, n, w.dr, w.dc);
+    join_df_kernel<<<unsigned(ceil_div(total, 256)), 256, 0, s>>>(w.Khi, w.Klo, w.W, total);
     UPDES_LAUNCH_CHECK();
     e = factor_core(n, w.W, w.ld, precision, nullptr, w.ld, w.piv, w.lu, s);
   } else {
-    split_df_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.K64, w.ld, w.F32, w.Wlo, w.ld, n,
-                                                                               w.dr, w.dc);
-    UPDES_LAUNCH_CHECK();
+    UPDES_CUDA_TRY(cudaMemcpyAsync(w.F32, w.Khi, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
+    UPDES_CUDA_TRY(cudaMemcpyAsync(w.Wlo, w.Klo, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
     e = factor_df_core(n, w.F32, w.Wlo, w.ld, w.piv, w.lu, s);
+    if (!e) e = diag_inverse(n, w.F32, w.ld, w.dinv, s);
   }
   if (e) return e;
   DeviceStatus h;
@@ -755,8 +871,11 @@ int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info,
   if (h.error) return h.error;
   info->lu_info = h.lu_info;
   info->t_factor_ms += t.stop();
-  const int32_t st3[3] = {n, precision, 1};
-  UPDES_CUDA_TRY(cudaMemcpyAsync(w.state, st3, sizeof st3, cudaMemcpyHostToDevice, s));
+  // {n, precision, valid, generation}: the generation tells derived copies of these factors (the batched
+  // solves' double-float planes) that they are stale after a refactorisation
+  static std::atomic<int32_t> generation{0};
+  const int32_t st4[4] = {n, precision, 1, generation.fetch_add(1) + 1};
+  UPDES_CUDA_TRY(cudaMemcpyAsync(w.state, st4, sizeof st4, cudaMemcpyHostToDevice, s));
   UPDES_CUDA_TRY(cudaStreamSynchronize(s));
   return UPDES_OK;
 }
@@ -774,10 +893,13 @@ int read_state(const SolveWs& w, int n, int* precision, cudaStream_t s) {
 int assemble_stage(const updes_problem* p, const SolveWs& w, int n, updes_solve_info* info, cudaStream_t s) {
   Timer t(s);
   int e;
-  if ((e = updes_assemble(p, w.K64, w.ld, nullptr, 0, s))) return e;
-  row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.K64, w.ld, n, w.dr);
+  if ((e = updes_assemble(p, w.W, w.ld, nullptr, 0, s))) return e;  // FP64 K, staged in the working buffer
+  row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.W, w.ld, n, w.dr);
   UPDES_LAUNCH_CHECK();
-  col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(w.K64, w.ld, n, w.dr, w.dc);
+  col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(w.W, w.ld, n, w.dr, w.dc);
+  UPDES_LAUNCH_CHECK();
+  split_df_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.W, w.ld, w.Khi, w.Klo, w.ld, n, w.dr,
+                                                                             w.dc);
   UPDES_LAUNCH_CHECK();
   info->t_assemble_ms += t.stop();
   return UPDES_OK;
@@ -987,6 +1109,41 @@ extern "C" int updes_lu_solve_noalloc(int32_t n, const void* F, int64_t ldf, int
   DeviceStatus h;
   if ((e = read_status(w.st, s, &h))) return e;
   return h.error;
+}
+
+// Views into a solve workspace (after updes_factor) for the batched solves.
+int solve_ws_views(const updes_problem* p, void* workspace, size_t workspace_bytes, const float** Khi,
+                   const float** Klo, const float** F32, const double** F64, int64_t* ld, const int32_t** piv,
+                   const double** dr, const double** dc, DeviceStatus** st, const int32_t** state) {
+  SolveWs w;
+  updes_solve_opts o;
+  int e = solve_setup(p, nullptr, workspace, workspace_bytes, &w, &o);
+  if (e) return e;
+  *Khi = w.Khi;
+  *Klo = w.Klo;
+  *F32 = w.F32;
+  *F64 = w.W;
+  *ld = w.ld;
+  *piv = w.piv;
+  *dr = w.dr;
+  *dc = w.dc;
+  *st = w.lu.st;
+  *state = w.state;
+  return UPDES_OK;
+}
+
+extern "C" int updes_workspace_status(const updes_problem* p, void* workspace, size_t workspace_bytes,
+                                      int32_t* error, void* stream) {
+  SolveWs w;
+  updes_solve_opts o;
+  int e = solve_setup(p, nullptr, workspace, workspace_bytes, &w, &o);
+  if (e) return e;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DeviceStatus h;
+  if ((e = read_status(w.lu.st, s, &h))) return e;
+  if (error) *error = h.error;
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.lu.st, 0, sizeof(DeviceStatus), s));
+  return UPDES_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -38,6 +38,9 @@ bool stats_timing() { return g_timing.load(std::memory_order_relaxed) != 0; }
 
 StatScope::StatScope(int c, cudaStream_t st, double fl, double by) : cat(c), s(st), ev0(nullptr), flops(fl), bytes(by) {
   if (!stats_timing()) return;
+  // no timing of work recorded into a CUDA graph (its events would never complete on their own)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
   cudaEvent_t a;
   if (cudaEventCreate(&a) == cudaSuccess) {
     cudaEventRecord(a, s);
