@@ -34,13 +34,15 @@ namespace {
 
 constexpr int TM = 128, TN = 64, TK = 64;
 constexpr int kDigits = 3, kGroups = 4;  // 8 digit products
-constexpr int kStages = 3;
+constexpr int kStages = 2;
 constexpr int kWarps = 10, kThreads = kWarps * 32, kEpiWarps = 8;
 constexpr uint32_t kTmemCols = 512;  // 2 sets x 4 groups x 64 columns
 constexpr int kATile = TM * TK * 2;  // 16 KB per digit plane
 constexpr int kBTile = TN * TK * 2;  //  8 KB per digit plane
 constexpr int kStageBytes = kDigits * (kATile + kBTile);  // 72 KB
-constexpr int kSmemBytes = kStages * kStageBytes + 1024;
+constexpr int kCHalf = TM * 32 * 4;                         // 16 KB: 128 rows x 32 FP32 (one 128-B swizzled box)
+constexpr int kCBytes = 4 * kCHalf;                         // C tile: {hi, lo} x {columns 0-31, 32-63}
+constexpr int kSmemBytes = kStages * kStageBytes + kCBytes + 1024;
 static_assert(kSmemBytes <= 227 * 1024, "shared memory");
 
 // instruction descriptor: D = F32, A = B = BF16, both K-major, N = 64, M = 128
@@ -168,6 +170,22 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+// 2-D tiled TMA load (x = column, y = row) completing on an mbarrier, and the matching bulk-group store.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(src)
+               : "memory");
+}
+
 // ---- digit pre-pass ------------------------------------------------------------------------------------
 // A (m x K, lda) -> Ad[p][r][k] (bf16, p < 3, k < Kp) and As[r][kb] = 2^(e-8), one warp per (row, k block).
 __global__ void digits_rows_kernel(const float* __restrict__ A, int64_t lda, int m, int K, int Kp,
@@ -242,17 +260,19 @@ __global__ void __launch_bounds__(256) digits_cols_kernel(const float* __restric
 
 // ---- main kernel ---------------------------------------------------------------------------------------
 struct Ctrl {
-  uint64_t full[kStages], empty[kStages], tfull[2], tempty[2];
+  uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], cfull, cfree, cready;
   uint32_t tmem;
   int abort_flag;
 };
 
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki3_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  const float* __restrict__ As, const float* __restrict__ Bs, float* __restrict__ Chi,
-                  float* __restrict__ Clo, int64_t ldc, int m, int nc, int Kp, DeviceStatus* st) {
+                  const __grid_constant__ CUtensorMap tmCh, const __grid_constant__ CUtensorMap tmCl,
+                  const float* __restrict__ As, const float* __restrict__ Bs, int m, int nc, int Kp,
+                  DeviceStatus* st) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sC = smem + kStages * kStageBytes;  // C tile, 128B-swizzled boxes: hi[0:32], hi[32:64], lo[0:32], lo[32:64]
   __shared__ Ctrl ctl;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tiles_n = int(ceil_div(nc, TN)), tiles_m = int(ceil_div(m, TM));
@@ -269,6 +289,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&ctl.tfull[s], 1);
       mbar_init(&ctl.tempty[s], kEpiWarps);
     }
+    mbar_init(&ctl.cfull, 1);
+    mbar_init(&ctl.cfree, 1);
+    mbar_init(&ctl.cready, kEpiWarps);
     ctl.abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -289,8 +312,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
-      int j = 0;
-      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmCh)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmCl)) : "memory");
+      int j = 0, tl = 0, last_c = -1;  // last_c: local index of the tile whose C load was issued last
+      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++tl) {
         const int r0 = (t / tiles_n) * TM, c0 = (t % tiles_n) * TN;
         for (int kb = 0; kb < nkb; ++kb, ++j) {
           const int s = j % kStages;
@@ -308,6 +333,20 @@ __global__ void __launch_bounds__(kThreads, 1)
             tma_load_3d(smem_u32(sA + p * kATile), &tmA, kb * TK, r0, p, &ctl.full[s]);
             tma_load_3d(smem_u32(sB + p * kBTile), &tmB, kb * TK, c0, p, &ctl.full[s]);
           }
+          if (kb == 0) {
+            // this tile's C (hi and lo planes), once the previous tile's C has been stored from the buffer
+            if (!mbar_wait(&ctl.cfree, (uint32_t(tl) & 1u) ^ 1u, abort_flag)) {
+              if (!*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 44); }
+              *abort_flag = 1;
+              break;
+            }
+            mbar_expect_tx(&ctl.cfull, uint32_t(kCBytes));
+            tma_load_2d(smem_u32(sC), &tmCh, c0, r0, &ctl.cfull);
+            tma_load_2d(smem_u32(sC + kCHalf), &tmCh, c0 + 32, r0, &ctl.cfull);
+            tma_load_2d(smem_u32(sC + 2 * kCHalf), &tmCl, c0, r0, &ctl.cfull);
+            tma_load_2d(smem_u32(sC + 3 * kCHalf), &tmCl, c0 + 32, r0, &ctl.cfull);
+            last_c = tl;
+          }
         }
       }
       if (*abort_flag) {
@@ -315,6 +354,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int jj = (j > kStages ? j - kStages : 0); jj < j; ++jj) {
           for (long long it = 0; it < (1 << 22); ++it) {
             if (mbar_try_wait(&ctl.full[jj % kStages], uint32_t(jj / kStages) & 1u)) break;
+            __nanosleep(64);
+          }
+        }
+        if (last_c >= 0) {
+          for (long long it = 0; it < (1 << 22); ++it) {
+            if (mbar_try_wait(&ctl.cfull, uint32_t(last_c) & 1u)) break;
             __nanosleep(64);
           }
         }
@@ -357,8 +402,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int row_in_tile = q * 32 + lane;
     const int colbase = h * 32;
     const uint32_t lane_base = uint32_t(q * 32) << 16;
-    int j = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int j = 0, tl = 0;
+    const bool storer = (warp == 2 && lane == 0);  // issues the C stores and frees the C buffer
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
       const int r0 = (t / tiles_n) * TM, c0 = (t % tiles_n) * TN;
       const int gr = r0 + row_in_tile;
       float acc_h[32], acc_l[32];
@@ -372,8 +418,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         const float sa = gr < m ? __ldg(As + int64_t(gr) * nkb + kb) : 0.f;
         const int my_c = c0 + colbase + lane;
         const float my_sb = my_c < nc ? __ldg(Bs + int64_t(my_c) * nkb + kb) : 0.f;
-        if (!mbar_wait(&ctl.tfull[set], tph, abort_flag)) {
-          if (!*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 43); }
+        // every wait ends in a warp vote, so a warp always leaves together (tcgen05.ld needs all 32 lanes)
+        if (!__all_sync(0xffffffffu, mbar_wait(&ctl.tfull[set], tph, abort_flag))) {
+          if (lane == 0 && !*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 43); }
           *abort_flag = 1;
           ok = false;
           break;
@@ -411,40 +458,57 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       if (!ok) break;
-      // ---- C -= acc for this thread's row and 32 columns ----
-      if (gr < m) {
-        float* ph = Chi + int64_t(gr) * ldc + c0 + colbase;
-        float* pl = Clo + int64_t(gr) * ldc + c0 + colbase;
-        const bool vec_c = (((reinterpret_cast<uintptr_t>(ph) | reinterpret_cast<uintptr_t>(pl)) & 15) == 0) &&
-                           c0 + colbase + 31 < nc;
-        if (vec_c) {
+      // ---- C -= acc in shared memory (the tile arrived by TMA), then one thread stores it back ----
+      if (!__all_sync(0xffffffffu, mbar_wait(&ctl.cfull, uint32_t(tl) & 1u, abort_flag))) {
+        if (lane == 0 && !*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 45); }
+        *abort_flag = 1;
+        break;
+      }
+      {
+        // this thread's row in the 128B-swizzled boxes: 16-byte chunk q of row r sits at chunk q ^ (r & 7)
+        const int r = row_in_tile;
+        uint8_t* hrow = sC + h * kCHalf + (r >> 3) * 1024 + (r & 7) * 128;
+        uint8_t* lrow = hrow + 2 * kCHalf;
 #pragma unroll
-          for (int qq = 0; qq < 8; ++qq) {
-            float4 hv = reinterpret_cast<float4*>(ph)[qq], lv = reinterpret_cast<float4*>(pl)[qq];
-            float hx[4] = {hv.x, hv.y, hv.z, hv.w}, lx[4] = {lv.x, lv.y, lv.z, lv.w};
+        for (int qq = 0; qq < 8; ++qq) {
+          const int off = ((qq ^ (r & 7)) << 4);
+          float4 hv = *reinterpret_cast<float4*>(hrow + off), lv = *reinterpret_cast<float4*>(lrow + off);
+          float hx[4] = {hv.x, hv.y, hv.z, hv.w}, lx[4] = {lv.x, lv.y, lv.z, lv.w};
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              float sx, tx;
-              two_sum(hx[u], -acc_h[qq * 4 + u], sx, tx);
-              tx = __fadd_rn(tx, __fsub_rn(lx[u], acc_l[qq * 4 + u]));
-              fast_two_sum(sx, tx, hx[u], lx[u]);
-            }
-            reinterpret_cast<float4*>(ph)[qq] = make_float4(hx[0], hx[1], hx[2], hx[3]);
-            reinterpret_cast<float4*>(pl)[qq] = make_float4(lx[0], lx[1], lx[2], lx[3]);
+          for (int u = 0; u < 4; ++u) {
+            float sx, tx;
+            two_sum(hx[u], -acc_h[qq * 4 + u], sx, tx);
+            tx = __fadd_rn(tx, __fsub_rn(lx[u], acc_l[qq * 4 + u]));
+            fast_two_sum(sx, tx, hx[u], lx[u]);
           }
-        } else {
-#pragma unroll
-          for (int u = 0; u < 32; ++u) {
-            if (c0 + colbase + u < nc) {
-              float sx, tx;
-              two_sum(ph[u], -acc_h[u], sx, tx);
-              tx = __fadd_rn(tx, __fsub_rn(pl[u], acc_l[u]));
-              fast_two_sum(sx, tx, ph[u], pl[u]);
-            }
-          }
+          *reinterpret_cast<float4*>(hrow + off) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+          *reinterpret_cast<float4*>(lrow + off) = make_float4(lx[0], lx[1], lx[2], lx[3]);
         }
       }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> visible to TMA
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&ctl.cready);
+      bool stop = false;
+      if (storer) {
+        if (!mbar_wait(&ctl.cready, uint32_t(tl) & 1u, abort_flag)) {
+          if (!*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 46); }
+          *abort_flag = 1;
+          stop = true;
+        }
+      }
+      if (storer && !stop) {
+        // rows >= m and columns >= nc are outside the tensor and are not written
+        tma_store_2d(&tmCh, c0, r0, smem_u32(sC));
+        tma_store_2d(&tmCh, c0 + 32, r0, smem_u32(sC + kCHalf));
+        tma_store_2d(&tmCl, c0, r0, smem_u32(sC + 2 * kCHalf));
+        tma_store_2d(&tmCl, c0 + 32, r0, smem_u32(sC + 3 * kCHalf));
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the buffer has been read
+        mbar_arrive(&ctl.cfree);
+      }
+      if (__any_sync(0xffffffffu, stop)) break;  // the whole warp leaves together
     }
+    if (storer) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete before exit
   }
 
   // ---- teardown: all roles done; make sure no MMA is in flight before tensor memory is freed ----
@@ -495,6 +559,20 @@ int make_map(CUtensorMap* map, void* base, int rows, int Kp, int box_rows) {
   return r == CUDA_SUCCESS ? UPDES_OK : UPDES_ERR_CUDA;
 }
 
+// 2-D map over an FP32 plane (rows x cols, row stride ld elements), box 32 columns x 128 rows, 128B swizzle
+int make_map_c(CUtensorMap* map, float* base, int rows, int cols, int64_t ld) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn) return UPDES_ERR_CUDA;
+  cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+  cuuint64_t strides[1] = {cuuint64_t(ld) * 4};
+  cuuint32_t box[2] = {32, cuuint32_t(TM)};
+  cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? UPDES_OK : UPDES_ERR_CUDA;
+}
+
 int num_sms_cached() {
   static int sms = 0;
   if (!sms) {
@@ -520,6 +598,9 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
   if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
   if (!scratch || scratch_bytes < ozaki3_scratch_bytes(m, nc, K)) return UPDES_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(scratch) & 255) != 0) return UPDES_ERR_INVALID;
+  // C goes through TMA: 16-byte aligned planes and row stride (else the caller uses the other kernel)
+  if (((reinterpret_cast<uintptr_t>(Chi) | reinterpret_cast<uintptr_t>(Clo)) & 15) != 0 || (ldc & 3) != 0)
+    return UPDES_ERR_UNSUPPORTED;
   const int Kp = int(ceil_div(K, TK)) * TK, nkb = Kp / TK;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   char* p = static_cast<char*>(scratch);
@@ -536,10 +617,12 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
     UPDES_CUDA_TRY(cudaFuncSetAttribute(ozaki3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     attr = true;
   }
-  CUtensorMap mapA, mapB;
+  CUtensorMap mapA, mapB, mapCh, mapCl;
   int e = make_map(&mapA, Ad, m, Kp, TM);
   if (e) return e;
   if ((e = make_map(&mapB, Bd, nc, Kp, TN))) return e;
+  if ((e = make_map_c(&mapCh, Chi, m, nc, ldc))) return e;
+  if ((e = make_map_c(&mapCl, Clo, m, nc, ldc))) return e;
 
   StatScope sc(kStatGemm, s, 2.0 * m * double(nc) * K, double(m) * nc * 16.0 + (double(m) + nc) * K * 4.0);
   {
@@ -551,7 +634,7 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
   }
   const int ntiles = int(ceil_div(m, TM) * ceil_div(nc, TN));
   const int grid = std::min(ntiles, num_sms_cached());
-  ozaki3_kernel<<<grid, kThreads, kSmemBytes, s>>>(mapA, mapB, As, Bs, Chi, Clo, ldc, m, nc, Kp, st);
+  ozaki3_kernel<<<grid, kThreads, kSmemBytes, s>>>(mapA, mapB, mapCh, mapCl, As, Bs, m, nc, Kp, st);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }

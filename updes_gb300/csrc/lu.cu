@@ -377,6 +377,256 @@ int num_sms() {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------------------------------
+// FP32 panel of the mixed LU with one exchange per column and look-ahead.
+//
+// G <= 32 CTAs each hold a block of the panel's rows in shared memory.  For every column j, each CTA
+// publishes one record: its best candidate (|a|, row) together with that row's 64 values, and the owner of
+// the diagonal position publishes the row sitting there.  A reader waits for the G tags and then fetches all
+// records in one round trip, so every CTA finds the pivot and both rows of the interchange without a second
+// exchange.  The records are published right after the look-ahead step (column j+1 updated and searched),
+// before the rank-1 update of the other columns, which then overlaps the exchange; a published row therefore
+// still lacks that last update for columns >= j+2, and readers apply it with the same fused multiply-add
+// (bitwise the same values as the owner's).
+struct alignas(16) PanelRec {
+  unsigned int tag;  // global column + 1 this record belongs to (written last)
+  int idx;           // candidate row (INT_MAX: none)
+  float absval;
+  float pad;
+  float row[kLuNb];
+};
+constexpr int kMaxPanelCtas = 32;
+
+__global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int64_t ld, int n, int k, int nb,
+                                                                  int rows_per_cta, int32_t* __restrict__ piv,
+                                                                  PanelRec* recs, int32_t* swap_map,
+                                                                  DeviceStatus* st) {
+  extern __shared__ __align__(16) unsigned char pf_smem[];
+  float(*crow)[kLuNb] = reinterpret_cast<float(*)[kLuNb]>(pf_smem);      // 32 x 64: the G records' rows
+  float* tile = reinterpret_cast<float*>(pf_smem) + (kMaxPanelCtas + 3) * kLuNb;  // rows_per_cta x nb
+  float* drow = crow[kMaxPanelCtas];                                      // 64: row at the diagonal position
+  float* prow = drow + kLuNb;                                             // 64: this column's pivot row
+  float* pprev = prow + kLuNb;                                            // 64: the previous column's pivot row
+  __shared__ float s_cval[kMaxPanelCtas];
+  __shared__ int s_cidx[kMaxPanelCtas];
+  __shared__ float red_v[kPanelThreads / 32];
+  __shared__ int red_i[kPanelThreads / 32];
+  __shared__ int s_best;  // local candidate (tile row) for the next column, -1 if none
+
+  const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int rbase = k + g * rows_per_cta;
+  const int rcount = max(0, min(rows_per_cta, n - rbase));
+  constexpr int kW = kPanelThreads / 32;
+
+  for (int l = wid; l < rcount; l += kW)
+    for (int c = lane; c < nb; c += 32) tile[int64_t(l) * nb + c] = W[int64_t(rbase + l) * ld + k + c];
+  __syncthreads();
+
+  // local argmax of column j over this CTA's rows with global index >= from (NaN wins; smallest row on ties)
+  auto local_best = [&](int j, int from) {
+    float bv = -1.f;
+    int bi = 0x7fffffff;
+    for (int l = max(0, from - rbase) + tid; l < rcount; l += blockDim.x) {
+      const float v = fabsf(tile[int64_t(l) * nb + j]);
+      const float vv = (v != v) ? INFINITY : v;
+      const int gr = rbase + l;
+      if (vv > bv || (vv == bv && gr < bi)) { bv = vv; bi = gr; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
+    if (lane == 0) { red_v[wid] = bv; red_i[wid] = bi; }
+    __syncthreads();
+    if (tid < 32) {
+      bv = tid < kW ? red_v[tid] : -1.f;
+      bi = tid < kW ? red_i[tid] : 0x7fffffff;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+      }
+      if (tid == 0) {
+        red_v[0] = bv;
+        red_i[0] = bi;
+        s_best = (bi == 0x7fffffff) ? -1 : bi - rbase;
+      }
+    }
+    __syncthreads();
+  };
+
+  // publish the records of column j (candidate; the diagonal row if this CTA owns position k + j)
+  auto publish = [&](int j) {
+    const int par = j & 1, diag = k + j;
+    PanelRec* mine = recs + par * (kMaxPanelCtas + 1) + g;
+    PanelRec* drec = recs + par * (kMaxPanelCtas + 1) + kMaxPanelCtas;
+    const bool own_diag = diag >= rbase && diag < rbase + rcount;
+    if (s_best >= 0 && tid < nb) __stcg(&mine->row[tid], tile[int64_t(s_best) * nb + tid]);
+    if (own_diag && tid >= 64 && tid < 64 + nb) __stcg(&drec->row[tid - 64], tile[int64_t(diag - rbase) * nb + tid - 64]);
+    if (tid == 0) {
+      __stcg(&mine->idx, red_i[0]);
+      __stcg(&mine->absval, red_v[0]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicExch(&mine->tag, unsigned(diag + 1));
+      if (own_diag) atomicExch(&drec->tag, unsigned(diag + 1));
+    }
+  };
+
+  local_best(0, k);
+  publish(0);
+  bool prev_ok = false;  // the previous column's pivot was usable, so its update is pending in published rows
+  for (int j = 0; j < nb; ++j) {
+    const int par = j & 1, diag = k + j;
+    const PanelRec* base = recs + par * (kMaxPanelCtas + 1);
+    // wait (bounded) for the G candidate records and the diagonal row
+    if (tid <= G) {
+      const PanelRec* r = (tid < G) ? base + tid : base + kMaxPanelCtas;
+      const volatile unsigned int* tw = &r->tag;
+      long long it = 0;
+      while (*tw != unsigned(diag + 1)) {
+        if (++it > kSpinLimit) {
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, 2);
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+    }
+    if (__syncthreads_or(*reinterpret_cast<volatile int*>(&st->error) != 0)) return;
+    // one round trip: every record's header and row, and the diagonal row
+    for (int e = tid; e < G * (kLuNb / 4); e += blockDim.x) {
+      const int w = e >> 4, q = e & 15;
+      reinterpret_cast<float4*>(crow[w])[q] = __ldcg(reinterpret_cast<const float4*>(base[w].row) + q);
+    }
+    if (tid < nb) drow[tid] = __ldcg(&base[kMaxPanelCtas].row[tid]);
+    if (tid < G) {
+      s_cval[tid] = __ldcg(&base[tid].absval);
+      s_cidx[tid] = __ldcg(&base[tid].idx);
+    }
+    __syncthreads();
+    // pivot: best over the G candidates (every warp computes it; no extra barrier)
+    float bv = lane < G ? s_cval[lane] : -1.f;
+    int bi = lane < G ? s_cidx[lane] : 0x7fffffff;
+    int bw = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      const int ow = __shfl_xor_sync(0xffffffffu, bw, o);
+      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; bw = ow; }
+    }
+    const int p = bi, gw = bw;
+    // the published rows still lack the previous column's update for columns >= j + 1
+    if (tid < nb) {
+      float pr = crow[gw][tid], dr = drow[tid];
+      if (prev_ok && tid > j) {
+        pr = __fmaf_rn(-crow[gw][j - 1], pprev[tid], pr);
+        dr = __fmaf_rn(-drow[j - 1], pprev[tid], dr);
+      }
+      prow[tid] = pr;
+      drow[tid] = dr;
+    }
+    __syncthreads();
+    const float pv = prow[j];
+    if (tid == 0 && g == 0) {
+      piv[diag] = (p == 0x7fffffff) ? diag : p;
+      if (pv == 0.f || !isfinite(pv)) atomicCAS(&st->lu_info, 0, diag + 1);
+    }
+    // interchange rows diag <-> p inside the panel
+    if (diag >= rbase && diag < rbase + rcount && tid < nb) tile[int64_t(diag - rbase) * nb + tid] = prow[tid];
+    if (p != diag && p >= rbase && p < rbase + rcount && tid < nb) tile[int64_t(p - rbase) * nb + tid] = drow[tid];
+    __syncthreads();
+    const int l0 = max(0, diag + 1 - rbase);
+    const bool ok = (pv != 0.f && isfinite(pv));
+    if (ok) {
+      const float rinv = 1.0f / pv;
+      for (int l = l0 + tid; l < rcount; l += blockDim.x) {
+        float* row = tile + int64_t(l) * nb;
+        row[j] *= rinv;
+        if (j + 1 < nb) row[j + 1] = __fmaf_rn(-row[j], prow[j + 1], row[j + 1]);  // look-ahead column
+      }
+    }
+    if (j + 1 < nb) {
+      __syncthreads();
+      local_best(j + 1, diag + 1);
+      publish(j + 1);
+    }
+    // rank-1 update of the remaining columns, overlapping the exchange of the next column
+    if (ok && j + 2 < nb) {
+      for (int l = l0 + wid; l < rcount; l += kW) {
+        float* row = tile + int64_t(l) * nb;
+        const float a = row[j];
+        for (int c = j + 2 + lane; c < nb; c += 32) row[c] = __fmaf_rn(-a, prow[c], row[c]);
+      }
+    }
+    if (tid < nb) pprev[tid] = prow[tid];
+    prev_ok = ok;
+    __syncthreads();
+  }
+  for (int l = wid; l < rcount; l += kW)
+    for (int c = lane; c < nb; c += 32) W[int64_t(rbase + l) * ld + k + c] = tile[int64_t(l) * nb + c];
+  if (swap_map && g == 0 && tid < 32) {
+    // net permutation of the interchanges piv[k, k+nb): content tracking over <= 2 nb rows
+    __shared__ int rows_s[128], cont_s[128];
+    for (int i = tid; i < nb; i += 32) rows_s[i] = cont_s[i] = k + i;
+    int cnt = nb;
+    __syncwarp();
+    for (int i = 0; i < nb; ++i) {
+      const int pp = piv[k + i];
+      if (pp == k + i) continue;
+      int found = -1;
+      for (int q = tid; q < cnt; q += 32)
+        if (rows_s[q] == pp) found = q;
+      found = __reduce_max_sync(0xffffffffu, found);
+      if (found < 0) {
+        if (tid == 0) { rows_s[cnt] = pp; cont_s[cnt] = pp; }
+        found = cnt++;
+        __syncwarp();
+      }
+      if (tid == 0) {
+        const int a = cont_s[i];
+        cont_s[i] = cont_s[found];
+        cont_s[found] = a;
+      }
+      __syncwarp();
+    }
+    for (int q = tid; q < cnt; q += 32) {
+      swap_map[1 + q] = rows_s[q];
+      swap_map[129 + q] = cont_s[q];
+    }
+    if (tid == 0) swap_map[0] = cnt;
+  }
+}
+
+// Launch the FP32 panel with G <= 32 CTAs when its rows fit; returns UPDES_ERR_UNSUPPORTED otherwise.
+int launch_panel_f32(float* W, int64_t ld, int n, int k, int w, int32_t* piv, PanelRec* recs, int32_t* swap_map,
+                     DeviceStatus* st, cudaStream_t s) {
+  const int m = n - k;
+  const int G = std::min(kMaxPanelCtas, int(ceil_div(m, 32)));
+  const int rows = int(ceil_div(m, G));
+  const size_t smem = (size_t(rows) * w + size_t(kMaxPanelCtas + 3) * kLuNb) * sizeof(float);
+  if (smem > 200 * 1024) return UPDES_ERR_UNSUPPORTED;
+  static bool attr = false;
+  if (!attr) {
+    UPDES_CUDA_TRY(cudaFuncSetAttribute(panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  int per_sm = 0;
+  UPDES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_f32_kernel, kPanelThreads, smem));
+  if (per_sm * num_sms() < G) return UPDES_ERR_UNSUPPORTED;
+  int k_ = k, nb_ = w, rows_ = rows, n_ = n;
+  int64_t ld_ = ld;
+  void* args[] = {&W, &ld_, &n_, &k_, &nb_, &rows_, &piv, &recs, &swap_map, &st};
+  StatScope sc(kStatPanel, s, double(m) * w * w, double(m) * w * 8.0);
+  UPDES_CUDA_TRY(cudaLaunchCooperativeKernel((void*)panel_f32_kernel, dim3(G), dim3(kPanelThreads), args, smem, s));
+  stats_count_launch(1);
+  return UPDES_OK;
+}
+
 size_t lu_panel_workspace_bytes(int nb) {
   const int G = 1024;  // upper bound on panel CTAs
   return 256 + sizeof(DeviceStatus) + 2 * G * sizeof(Cand) + 2ull * G * nb * sizeof(double) + 2ull * nb * sizeof(double);
@@ -446,6 +696,10 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     return !(v && v[0] == '3');
   }();
   UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256 + 2 * 1024 * sizeof(Cand), s));  // barrier words and candidate tags
+  // the single-exchange panel's records live in the candidate-row area (tags must start at zero)
+  PanelRec* recs = reinterpret_cast<PanelRec*>(cand_row);
+  static_assert(2 * (kMaxPanelCtas + 1) * sizeof(PanelRec) <= 2 * 1024 * kLuNb * sizeof(double), "panel records");
+  UPDES_CUDA_TRY(cudaMemsetAsync(recs, 0, 2 * (kMaxPanelCtas + 1) * sizeof(PanelRec), s));
   constexpr int kOuter = kOuterNb;
   auto swaps = [&](int k, int w) -> int {
     SwapJobs j{};
@@ -479,10 +733,12 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   };
   auto upd = [&](int r0, int r1, int c0, int c1, int kk0, int kk1) -> int {
     // W[r0:r1, c0:c1] -= F[r0:r1, kk0:kk1] * F[kk0:kk1, c0:c1]
-    if (!use_v2)
-      return ozaki3_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld, Whi + int64_t(r0) * ld + kk0,
-                           ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0, c1 - c0, kk1 - kk0, digits, digits_bytes, st,
-                           s);
+    if (!use_v2) {
+      const int e3 = ozaki3_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld,
+                                   Whi + int64_t(r0) * ld + kk0, ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0,
+                                   c1 - c0, kk1 - kk0, digits, digits_bytes, st, s);
+      if (e3 != UPDES_ERR_UNSUPPORTED) return e3;
+    }
     return ozaki_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld, Whi + int64_t(r0) * ld + kk0,
                         ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0, c1 - c0, kk1 - kk0, st, s);
   };
@@ -491,9 +747,11 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     const int KE = std::min(K0 + kOuter, n);
     for (int k = K0; k < KE; k += nb) {
       const int w = std::min(nb, KE - k);
-      if ((e = launch_panel<float, true>(Whi, Wlo, ld, Whi, ld, n, k, w, piv, bar, cand, cand_row, diag_row,
-                                         swap_map, st, s)))
-        return e;
+      e = launch_panel_f32(Whi, ld, n, k, w, piv, recs, swap_map, st, s);
+      if (e == UPDES_ERR_UNSUPPORTED)
+        e = launch_panel<float, true>(Whi, Wlo, ld, Whi, ld, n, k, w, piv, bar, cand, cand_row, diag_row, swap_map,
+                                      st, s);
+      if (e) return e;
       if ((e = swaps(k, w))) return e;
       if (k + w < KE) {
         if ((e = trsm(k, w, k + w, KE))) return e;
@@ -523,6 +781,10 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
   double* cand_row = reinterpret_cast<double*>(base + 256 + 2 * 1024 * sizeof(Cand));
   double* diag_row = cand_row + 2ll * 1024 * nb;
   UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256 + 2 * 1024 * sizeof(Cand), s));  // barrier words and candidate tags
+  // the single-exchange panel's records live in the candidate-row area (tags must start at zero)
+  PanelRec* recs = reinterpret_cast<PanelRec*>(cand_row);
+  static_assert(2 * (kMaxPanelCtas + 1) * sizeof(PanelRec) <= 2 * 1024 * kLuNb * sizeof(double), "panel records");
+  UPDES_CUDA_TRY(cudaMemsetAsync(recs, 0, 2 * (kMaxPanelCtas + 1) * sizeof(PanelRec), s));
   for (int k = 0; k < n; k += nb) {
     const int w = std::min(nb, n - k);
     {
