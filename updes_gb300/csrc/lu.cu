@@ -690,10 +690,11 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   const int64_t scratch_ld = int64_t(n) + 64;
   void* digits = after + 2048 + lu_df_swap_bytes(n);
   const size_t digits_bytes = ozaki3_scratch_bytes(n, n, kOuterNb);
-  // UPDES_OZAKI=3 selects the persistent TMA-fed update (gemm_tc3.cu) instead of gemm_tc.cu's
+  // the persistent TMA-fed update (gemm_tc3.cu); UPDES_OZAKI=2 selects the per-tile kernel of gemm_tc.cu, which
+  // also serves updates whose C planes are not 16-byte aligned
   static const bool use_v2 = [] {
     const char* v = std::getenv("UPDES_OZAKI");
-    return !(v && v[0] == '3');
+    return v && v[0] == '2';
   }();
   UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256 + 2 * 1024 * sizeof(Cand), s));  // barrier words and candidate tags
   // the single-exchange panel's records live in the candidate-row area (tags must start at zero)
