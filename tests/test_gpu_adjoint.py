@@ -60,7 +60,9 @@ def test_adjoint_matches_central_differences():
     factors are reused and that noise is about 1e-6 of the derivative (bound 1e-5); along the fields K
     itself changes and is refactored, whose rounding (about 1e-11 of J on this r^5 system) gives about
     1e-4 of the derivative (bound 1e-3).  At h = 1e-4 the fields' quotient is pinned at 1e-6 (O(h^2)
-    truncation).  The FP32 path's adjoint is checked along the control at h = 1e-2.
+    truncation).  The FP32 path's adjoint is checked along the control at h = 1e-2: each of its solves stops at
+    a backward error of 256 FP64 unit roundoffs, so two perturbed solves differ by about 1e-10 of J and the
+    quotient by about 1e-8 of the derivative (bound 1e-7).
     """
     g = load("adjoint_kgrad_10x10")
     case = C.CASES[C.ADJOINT_CASE]
@@ -86,4 +88,4 @@ def test_adjoint_matches_central_differences():
     assert abs(fd_f("fp64", 1e-4) - gf) <= 1e-6 * abs(gf)
     assert abs(fd_f("fp64", 1e-6) - gf) <= 1e-3 * abs(gf)
     J32, dc32, _ = _loss("fp32")
-    assert abs(fd_c("fp32", 1e-2) - dc32 @ v) <= 1e-8 * abs(dc32 @ v)
+    assert abs(fd_c("fp32", 1e-2) - dc32 @ v) <= 1e-7 * abs(dc32 @ v)

@@ -443,17 +443,20 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const float sb = __shfl_sync(0xffffffffu, my_sb, ch * 8 + u);
-            float hh, ll, e;
+            // k-block value = g0 + 2^-9 g1 + 2^-18 (g2 + 2^-9 g3): g0 + 2^-9 g1 exactly as (hh, ll); the two
+            // small groups merged in one rounding (about 2^-40 of the block's scale, far below the digit cut)
+            float hh, ll;
             two_sum(g[0][u], __fmul_rn(g[1][u], 1.953125e-3f), hh, ll);
-            two_sum(hh, __fmul_rn(g[2][u], 3.814697265625e-06f), hh, e);
-            ll = __fadd_rn(ll, __fadd_rn(e, __fmul_rn(g[3][u], 7.450580596923828e-09f)));
+            const float g23 = __fmaf_rn(g[3][u], 1.953125e-3f, g[2][u]);
+            ll = __fmaf_rn(g23, 3.814697265625e-06f, ll);
             const float sc = __fmul_rn(sa, sb);  // power of two: exact
             hh = __fmul_rn(hh, sc);
             ll = __fmul_rn(ll, sc);
+            // acc += (hh, ll); the low word is renormalised by the final update of C (K <= 1024: at most 16 blocks)
             float s1, t1;
             two_sum(acc_h[ch * 8 + u], hh, s1, t1);
-            t1 = __fadd_rn(t1, __fadd_rn(acc_l[ch * 8 + u], ll));
-            fast_two_sum(s1, t1, acc_h[ch * 8 + u], acc_l[ch * 8 + u]);
+            acc_h[ch * 8 + u] = s1;
+            acc_l[ch * 8 + u] = __fadd_rn(acc_l[ch * 8 + u], __fadd_rn(t1, ll));
           }
         }
       }
@@ -596,6 +599,8 @@ size_t ozaki3_scratch_bytes(int mmax, int ncmax, int Kmax) {
 int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
                   int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s) {
   if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
+  // the tile accumulator's low word is left unnormalised across k blocks: a few blocks only
+  if (K > 1024) return UPDES_ERR_UNSUPPORTED;
   if (!scratch || scratch_bytes < ozaki3_scratch_bytes(m, nc, K)) return UPDES_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(scratch) & 255) != 0) return UPDES_ERR_INVALID;
   // C goes through TMA: 16-byte aligned planes and row stride (else the caller uses the other kernel)

@@ -223,29 +223,30 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
   }
 }
 
-// Row interchanges as a gather/scatter through a scratch buffer, for up to 3 (plane, column range) jobs.
+// Row interchanges of up to 3 (plane, column range) jobs.
 struct SwapJobs {
   float* plane[3];
   int64_t c0[3], c1[3];
   int njobs;
 };
 
-__global__ void swap_gather_kernel(SwapJobs jobs, int64_t ld, const int32_t* __restrict__ map, float* scratch,
-                                   int64_t scratch_ld) {
-  const int q = blockIdx.y, j = blockIdx.z;
-  if (j >= jobs.njobs || q >= map[0]) return;
-  const int64_t c = jobs.c0[j] + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (c >= jobs.c1[j]) return;
-  scratch[(int64_t(j) * 128 + q) * scratch_ld + (c - jobs.c0[j])] = jobs.plane[j][int64_t(map[129 + q]) * ld + c];
-}
-
-__global__ void swap_scatter_kernel(SwapJobs jobs, int64_t ld, const int32_t* __restrict__ map, const float* scratch,
-                                    int64_t scratch_ld) {
-  const int q = blockIdx.y, j = blockIdx.z;
-  if (j >= jobs.njobs || q >= map[0]) return;
-  const int64_t c = jobs.c0[j] + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (c >= jobs.c1[j]) return;
-  jobs.plane[j][int64_t(map[1 + q]) * ld + c] = scratch[(int64_t(j) * 128 + q) * scratch_ld + (c - jobs.c0[j])];
+// All row interchanges of a panel in one pass: a CTA per (64-column chunk, job) reads the moved rows of its
+// columns into shared memory, then writes each to its destination (the net permutation from the panel's swap
+// map), so a launch touches only the rows that move.
+__global__ void __launch_bounds__(256) swap_rows_kernel(SwapJobs jobs, int64_t ld, const int32_t* __restrict__ map) {
+  __shared__ float buf[128][64];
+  const int j = blockIdx.y;
+  if (j >= jobs.njobs) return;
+  const int cnt = map[0];
+  const int col = threadIdx.x & 63, r0 = threadIdx.x >> 6;
+  const int64_t c = jobs.c0[j] + int64_t(blockIdx.x) * 64 + col;
+  const bool ok = c < jobs.c1[j];
+  float* plane = jobs.plane[j];
+  for (int q = r0; q < cnt; q += 4)
+    if (ok) buf[q][col] = plane[int64_t(map[129 + q]) * ld + c];
+  __syncthreads();
+  for (int q = r0; q < cnt; q += 4)
+    if (ok) plane[int64_t(map[1 + q]) * ld + c] = buf[q][col];
 }
 
 // U = L^-1 W on rows [k, k+nb), columns [c0, c1): L unit lower from F (FP32), W double-float.  Each row is
@@ -279,6 +280,69 @@ __global__ void __launch_bounds__(64) trsm_df_kernel(float* Whi, const float* Wl
     const float xi = __fadd_rn(sh, sl);
     sX[i][t] = xi;
     Whi[idx] = xi;
+  }
+}
+
+// U12 = L11^-1 W12 for a full 64-row panel: 64 columns per CTA, 4 lanes per column.  The right-hand sides
+// (double-float planes) are staged in shared memory in one coalesced pass; lane s of a column's group keeps
+// rows s, s+4, ..., s+60 in registers.  Step j (unrolled): the owner of row j rounds it to FP32 (the factor
+// entry), broadcasts it by shuffle, and every lane subtracts L[i][j] * x_j from its rows i > j in
+// double-float arithmetic; the chain is one shuffle per row instead of a 2016-term dependent sum.
+struct TrsmDfSmem {
+  float L[64][65];
+  float Xh[64][65], Xl[64][65];
+};
+
+__global__ void __launch_bounds__(256) trsm_df64_kernel(float* Whi, const float* Wlo, int64_t ld, int k, int64_t c0,
+                                                        int64_t c1) {
+  extern __shared__ float4 trsm_df_smem[];
+  TrsmDfSmem& sm = *reinterpret_cast<TrsmDfSmem*>(trsm_df_smem);
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int64_t cb = c0 + int64_t(blockIdx.x) * 64;
+  for (int e = tid; e < 64 * 64; e += blockDim.x) {
+    const int i = e >> 6, j = e & 63;
+    sm.L[i][j] = (j < i) ? Whi[int64_t(k + i) * ld + k + j] : 0.f;
+    const int64_t c = cb + j;
+    const bool ok = c < c1;
+    sm.Xh[i][j] = ok ? Whi[int64_t(k + i) * ld + c] : 0.f;
+    sm.Xl[i][j] = ok ? Wlo[int64_t(k + i) * ld + c] : 0.f;
+  }
+  __syncthreads();
+  const int col = tid >> 2, s = tid & 3;
+  const int gbase = lane & ~3;
+  float ah[16], al[16];
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    ah[r] = sm.Xh[s + 4 * r][col];
+    al[r] = sm.Xl[s + 4 * r][col];
+  }
+#pragma unroll
+  for (int j = 0; j < 64; ++j) {
+    // row j lives in slot j / 4 of lane j % 4
+    const float mine = __fadd_rn(ah[j >> 2], al[j >> 2]);
+    const float xj = __shfl_sync(0xffffffffu, mine, gbase | (j & 3));
+    if (s == (j & 3)) sm.Xh[j][col] = xj;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      if (4 * r + 3 <= j) continue;  // every row of this slot is <= j
+      const int i = s + 4 * r;
+      if (i > j) {
+        const float f = -sm.L[i][j];
+        const float p = __fmul_rn(f, xj);
+        const float e = __fmaf_rn(f, xj, -p);
+        const float t0 = __fadd_rn(ah[r], p);
+        const float bb = __fsub_rn(t0, ah[r]);
+        const float tt = __fadd_rn(__fsub_rn(ah[r], __fsub_rn(t0, bb)), __fsub_rn(p, bb));
+        ah[r] = t0;
+        al[r] = __fadd_rn(al[r], __fadd_rn(tt, e));
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < 64 * 64; e += blockDim.x) {
+    const int i = e >> 6, j = e & 63;
+    const int64_t c = cb + j;
+    if (c < c1) Whi[int64_t(k + i) * ld + c] = sm.Xh[i][j];
   }
 }
 
@@ -403,7 +467,9 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
                                                                   DeviceStatus* st) {
   extern __shared__ __align__(16) unsigned char pf_smem[];
   float(*crow)[kLuNb] = reinterpret_cast<float(*)[kLuNb]>(pf_smem);      // 32 x 64: the G records' rows
-  float* tile = reinterpret_cast<float*>(pf_smem) + (kMaxPanelCtas + 3) * kLuNb;  // rows_per_cta x nb
+  // rows_per_cta x nb with row stride nb + 1: consecutive rows of one column fall in different banks
+  float* tile = reinterpret_cast<float*>(pf_smem) + (kMaxPanelCtas + 3) * kLuNb;
+  const int ldt = nb + 1;
   float* drow = crow[kMaxPanelCtas];                                      // 64: row at the diagonal position
   float* prow = drow + kLuNb;                                             // 64: this column's pivot row
   float* pprev = prow + kLuNb;                                            // 64: the previous column's pivot row
@@ -419,7 +485,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
   constexpr int kW = kPanelThreads / 32;
 
   for (int l = wid; l < rcount; l += kW)
-    for (int c = lane; c < nb; c += 32) tile[int64_t(l) * nb + c] = W[int64_t(rbase + l) * ld + k + c];
+    for (int c = lane; c < nb; c += 32) tile[int64_t(l) * ldt + c] = W[int64_t(rbase + l) * ld + k + c];
   __syncthreads();
 
   // local argmax of column j over this CTA's rows with global index >= from (NaN wins; smallest row on ties)
@@ -427,7 +493,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
     float bv = -1.f;
     int bi = 0x7fffffff;
     for (int l = max(0, from - rbase) + tid; l < rcount; l += blockDim.x) {
-      const float v = fabsf(tile[int64_t(l) * nb + j]);
+      const float v = fabsf(tile[int64_t(l) * ldt + j]);
       const float vv = (v != v) ? INFINITY : v;
       const int gr = rbase + l;
       if (vv > bv || (vv == bv && gr < bi)) { bv = vv; bi = gr; }
@@ -462,8 +528,8 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
     PanelRec* mine = recs + par * (kMaxPanelCtas + 1) + g;
     PanelRec* drec = recs + par * (kMaxPanelCtas + 1) + kMaxPanelCtas;
     const bool own_diag = diag >= rbase && diag < rbase + rcount;
-    if (s_best >= 0 && tid < nb) __stcg(&mine->row[tid], tile[int64_t(s_best) * nb + tid]);
-    if (own_diag && tid >= 64 && tid < 64 + nb) __stcg(&drec->row[tid - 64], tile[int64_t(diag - rbase) * nb + tid - 64]);
+    if (s_best >= 0 && tid < nb) __stcg(&mine->row[tid], tile[int64_t(s_best) * ldt + tid]);
+    if (own_diag && tid >= 64 && tid < 64 + nb) __stcg(&drec->row[tid - 64], tile[int64_t(diag - rbase) * ldt + tid - 64]);
     if (tid == 0) {
       __stcg(&mine->idx, red_i[0]);
       __stcg(&mine->absval, red_v[0]);
@@ -537,15 +603,15 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
       if (pv == 0.f || !isfinite(pv)) atomicCAS(&st->lu_info, 0, diag + 1);
     }
     // interchange rows diag <-> p inside the panel
-    if (diag >= rbase && diag < rbase + rcount && tid < nb) tile[int64_t(diag - rbase) * nb + tid] = prow[tid];
-    if (p != diag && p >= rbase && p < rbase + rcount && tid < nb) tile[int64_t(p - rbase) * nb + tid] = drow[tid];
+    if (diag >= rbase && diag < rbase + rcount && tid < nb) tile[int64_t(diag - rbase) * ldt + tid] = prow[tid];
+    if (p != diag && p >= rbase && p < rbase + rcount && tid < nb) tile[int64_t(p - rbase) * ldt + tid] = drow[tid];
     __syncthreads();
     const int l0 = max(0, diag + 1 - rbase);
     const bool ok = (pv != 0.f && isfinite(pv));
     if (ok) {
       const float rinv = 1.0f / pv;
       for (int l = l0 + tid; l < rcount; l += blockDim.x) {
-        float* row = tile + int64_t(l) * nb;
+        float* row = tile + int64_t(l) * ldt;
         row[j] *= rinv;
         if (j + 1 < nb) row[j + 1] = __fmaf_rn(-row[j], prow[j + 1], row[j + 1]);  // look-ahead column
       }
@@ -557,10 +623,37 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
     }
     // rank-1 update of the remaining columns, overlapping the exchange of the next column
     if (ok && j + 2 < nb) {
-      for (int l = l0 + wid; l < rcount; l += kW) {
-        float* row = tile + int64_t(l) * nb;
-        const float a = row[j];
-        for (int c = j + 2 + lane; c < nb; c += 32) row[c] = __fmaf_rn(-a, prow[c], row[c]);
+      // warp w takes rows l0 + w + 8i, four at a time for independent shared-memory traffic; lanes span columns
+      const float p0 = (j + 2 + lane < nb) ? prow[j + 2 + lane] : 0.f;
+      const float p1 = (j + 34 + lane < nb) ? prow[j + 34 + lane] : 0.f;
+      const int c0 = j + 2 + lane, c1 = j + 34 + lane;
+      int l = l0 + wid;
+      for (; l + 3 * kW < rcount; l += 4 * kW) {
+        float* r0 = tile + int64_t(l) * ldt;
+        float* r1 = r0 + kW * ldt;
+        float* r2 = r1 + kW * ldt;
+        float* r3 = r2 + kW * ldt;
+        const float a0 = r0[j], a1 = r1[j], a2 = r2[j], a3 = r3[j];
+        if (c0 < nb) {
+          const float x0 = r0[c0], x1 = r1[c0], x2 = r2[c0], x3 = r3[c0];
+          r0[c0] = __fmaf_rn(-a0, p0, x0);
+          r1[c0] = __fmaf_rn(-a1, p0, x1);
+          r2[c0] = __fmaf_rn(-a2, p0, x2);
+          r3[c0] = __fmaf_rn(-a3, p0, x3);
+        }
+        if (c1 < nb) {
+          const float x0 = r0[c1], x1 = r1[c1], x2 = r2[c1], x3 = r3[c1];
+          r0[c1] = __fmaf_rn(-a0, p1, x0);
+          r1[c1] = __fmaf_rn(-a1, p1, x1);
+          r2[c1] = __fmaf_rn(-a2, p1, x2);
+          r3[c1] = __fmaf_rn(-a3, p1, x3);
+        }
+      }
+      for (; l < rcount; l += kW) {
+        float* r0 = tile + int64_t(l) * ldt;
+        const float a0 = r0[j];
+        if (c0 < nb) r0[c0] = __fmaf_rn(-a0, p0, r0[c0]);
+        if (c1 < nb) r0[c1] = __fmaf_rn(-a0, p1, r0[c1]);
       }
     }
     if (tid < nb) pprev[tid] = prow[tid];
@@ -568,7 +661,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
     __syncthreads();
   }
   for (int l = wid; l < rcount; l += kW)
-    for (int c = lane; c < nb; c += 32) W[int64_t(rbase + l) * ld + k + c] = tile[int64_t(l) * nb + c];
+    for (int c = lane; c < nb; c += 32) W[int64_t(rbase + l) * ld + k + c] = tile[int64_t(l) * ldt + c];
   if (swap_map && g == 0 && tid < 32) {
     // net permutation of the interchanges piv[k, k+nb): content tracking over <= 2 nb rows
     __shared__ int rows_s[128], cont_s[128];
@@ -608,7 +701,7 @@ int launch_panel_f32(float* W, int64_t ld, int n, int k, int w, int32_t* piv, Pa
   const int m = n - k;
   const int G = std::min(kMaxPanelCtas, int(ceil_div(m, 32)));
   const int rows = int(ceil_div(m, G));
-  const size_t smem = (size_t(rows) * w + size_t(kMaxPanelCtas + 3) * kLuNb) * sizeof(float);
+  const size_t smem = (size_t(rows) * (w + 1) + size_t(kMaxPanelCtas + 3) * kLuNb) * sizeof(float);
   if (smem > 200 * 1024) return UPDES_ERR_UNSUPPORTED;
   static bool attr = false;
   if (!attr) {
@@ -666,13 +759,9 @@ int launch_panel(void* W, const float* Wlo, int64_t ldw, TF* F, int64_t ldf, int
 
 constexpr int kOuterNb = 4 * kLuNb;  // 256: width of the big exact trailing updates
 
-size_t lu_df_swap_bytes(int n) { return (3ull * 128 * (size_t(n) + 64) * sizeof(float) + 255) & ~size_t(255); }
-
 size_t lu_df_workspace_bytes(int n) {
-  // panel scratch (rounded up to 256 B), 2 KB swap map, 3 x 128 rows of swap scratch, digit scratch of the
-  // tensor-core update
-  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + 2048 + lu_df_swap_bytes(n) +
-         ozaki3_scratch_bytes(n, n, kOuterNb);
+  // panel scratch (rounded up to 256 B), 2 KB swap map, digit scratch of the tensor-core update
+  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + 2048 + ozaki3_scratch_bytes(n, n, kOuterNb);
 }
 
 int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* ws, size_t ws_bytes, DeviceStatus* st,
@@ -686,9 +775,7 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   double* diag_row = cand_row + 2ll * 1024 * nb;
   char* after = base + ((lu_panel_workspace_bytes(nb) + 255) & ~size_t(255));
   int32_t* swap_map = reinterpret_cast<int32_t*>(after);
-  float* scratch = reinterpret_cast<float*>(after + 2048);
-  const int64_t scratch_ld = int64_t(n) + 64;
-  void* digits = after + 2048 + lu_df_swap_bytes(n);
+  void* digits = after + 2048;
   const size_t digits_bytes = ozaki3_scratch_bytes(n, n, kOuterNb);
   // the persistent TMA-fed update (gemm_tc3.cu); UPDES_OZAKI=2 selects the per-tile kernel of gemm_tc.cu, which
   // also serves updates whose C planes are not 16-byte aligned
@@ -717,18 +804,25 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     }
     j.njobs = nj;
     if (!nj) return UPDES_OK;
-    dim3 grid(unsigned(ceil_div(maxc, 256)), 128, nj);
     StatScope sc(kStatOther, s, 0.0, 2.0 * 2 * w * maxc * 4.0 * nj);
-    swap_gather_kernel<<<grid, 256, 0, s>>>(j, ld, swap_map, scratch, scratch_ld);
-    UPDES_LAUNCH_CHECK();
-    swap_scatter_kernel<<<grid, 256, 0, s>>>(j, ld, swap_map, scratch, scratch_ld);
+    swap_rows_kernel<<<dim3(unsigned(ceil_div(maxc, 64)), nj), 256, 0, s>>>(j, ld, swap_map);
     UPDES_LAUNCH_CHECK();
     return UPDES_OK;
   };
   auto trsm = [&](int k, int w, int64_t c0, int64_t c1) -> int {
     if (c1 <= c0) return UPDES_OK;
     StatScope sc(kStatTrsm, s, double(w) * w * (c1 - c0), double(w) * (c1 - c0) * 12.0);
-    trsm_df_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 64, 0, s>>>(Whi, Wlo, ld, k, w, c0, c1);
+    if (w == 64) {
+      static bool attr = false;
+      if (!attr) {
+        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsm_df64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            int(sizeof(TrsmDfSmem))));
+        attr = true;
+      }
+      trsm_df64_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 256, sizeof(TrsmDfSmem), s>>>(Whi, Wlo, ld, k, c0, c1);
+    } else {
+      trsm_df_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 64, 0, s>>>(Whi, Wlo, ld, k, w, c0, c1);
+    }
     UPDES_LAUNCH_CHECK();
     return UPDES_OK;
   };
@@ -849,6 +943,21 @@ __device__ __forceinline__ void df_fma(float f, float xh, float xl, float& sh, f
   t = __fadd_rn(t, __fadd_rn(sl, __fmaf_rn(f, xl, e)));
   sh = __fadd_rn(s, t);  // renormalised after every term
   sl = __fsub_rn(t, __fsub_rn(sh, s));
+}
+
+// Warp-wide sum of a double-float pair with FP32 instructions (FP64 adds would queue on the SM's few FP64
+// units): every lane ends with the total.
+__device__ __forceinline__ void df_warp_sum(float& h, float& l) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    const float s = __fadd_rn(h, oh);
+    const float bb = __fsub_rn(s, h);
+    float t = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(oh, bb));
+    t = __fadd_rn(t, __fadd_rn(l, ol));
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+  }
 }
 
 // (qh, ql) = (bh + bl) / d for an FP32 divisor d
@@ -982,23 +1091,38 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
     }
     __syncthreads();
   }
-  // row sums of the off-diagonal part
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    double v = (sizeof(TF) == 4) ? double(ah[i]) + double(al[i]) : ad[i];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sacc[warp * 8 + i] = v;
-  }
   if constexpr (sizeof(TF) == 4) {
     if (dinv) {
+      // row sums of the off-diagonal part in double-float (FP32 pipes), kept as two FP32 words
+      float* sacc_h = reinterpret_cast<float*>(sacc);
+      float* sacc_l = sacc_h + kTB;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        float h = ah[i], l = al[i];
+        df_warp_sum(h, l);
+        if (lane == 0) {
+          sacc_h[warp * 8 + i] = h;
+          sacc_l[warp * 8 + i] = l;
+        }
+      }
       // x_blk = D (b - off-diagonal part), D the inverted diagonal block (double-float planes, prefetched):
       // a matvec, no dependent chain
       __syncthreads();
       if (tid < kTB) {
-        const double v = tid < rows ? b_own - sacc[tid] : 0.0;
-        const float hh = float(v);
-        sxh[tid] = hh;
-        sxl[tid] = float(v - double(hh));
+        // b - acc in double-float: b split once, then a two-sum
+        const float bh = float(b_own), bl = float(b_own - double(bh));
+        float rh = 0.f, rl = 0.f;
+        if (tid < rows) {
+          const float ch = -sacc_h[tid], cl = -sacc_l[tid];
+          const float s0 = __fadd_rn(bh, ch);
+          const float bb = __fsub_rn(s0, bh);
+          float t = __fadd_rn(__fsub_rn(bh, __fsub_rn(s0, bb)), __fsub_rn(ch, bb));
+          t = __fadd_rn(t, __fadd_rn(bl, cl));
+          rh = __fadd_rn(s0, t);
+          rl = __fsub_rn(t, __fsub_rn(rh, s0));
+        }
+        sxh[tid] = rh;
+        sxl[tid] = rl;
       }
       __syncthreads();
 #pragma unroll
@@ -1019,9 +1143,8 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
           ph = __fadd_rn(s0, t);
           pl = __fsub_rn(t, __fsub_rn(ph, s0));
         }
-        double v = double(ph) + double(pl);
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0 && rr < rows) x[r0 + rr] = v;
+        df_warp_sum(ph, pl);
+        if (lane == 0 && rr < rows) x[r0 + rr] = double(ph) + double(pl);
       }
       __syncthreads();
       if (tid == 0) {
@@ -1030,6 +1153,13 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
       }
       return;
     }
+  }
+  // row sums of the off-diagonal part
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    double v = (sizeof(TF) == 4) ? double(ah[i]) + double(al[i]) : ad[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sacc[warp * 8 + i] = v;
   }
   // diagonal block
   {

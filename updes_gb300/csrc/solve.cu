@@ -67,12 +67,25 @@ __global__ void row_scale_kernel(const double* __restrict__ K, int64_t ld, int n
   }
 }
 
-__global__ void col_scale_kernel(const double* __restrict__ K, int64_t ld, int n, const double* __restrict__ dr,
-                                 double* __restrict__ dc) {
+// Column maxima of |K| diag(dr) over a chunk of rows per blockIdx.y, combined with an integer atomicMax on the
+// bit patterns (non-negative doubles order like their bits); colmax must start at zero.
+constexpr int kColScaleChunks = 64;
+__global__ void col_max_kernel(const double* __restrict__ K, int64_t ld, int n, const double* __restrict__ dr,
+                               unsigned long long* __restrict__ colmax) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
+  const int rows = int(ceil_div(n, kColScaleChunks));
+  const int i0 = blockIdx.y * rows, i1 = min(n, i0 + rows);
   double m = 0.0;
-  for (int i = 0; i < n; ++i) m = fmax(m, fabs(K[int64_t(i) * ld + j]) * dr[i]);
+  for (int i = i0; i < i1; ++i) m = fmax(m, fabs(K[int64_t(i) * ld + j]) * dr[i]);
+  if (m > 0.0) atomicMax(colmax + j, (unsigned long long)__double_as_longlong(m));
+}
+
+// dc_j = 2^-e with max_i |K_ij| dr_i in [2^(e-1), 2^e)  (dc holds the maxima' bits on entry)
+__global__ void col_scale_kernel(int n, double* __restrict__ dc) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double m = __longlong_as_double((long long)reinterpret_cast<unsigned long long*>(dc)[j]);
   int e = 0;
   if (m > 0.0 && isfinite(m)) frexp(m, &e);
   dc[j] = ldexp(1.0, -e);
@@ -896,7 +909,11 @@ int assemble_stage(const updes_problem* p, const SolveWs& w, int n, updes_solve_
   if ((e = updes_assemble(p, w.W, w.ld, nullptr, 0, s))) return e;  // FP64 K, staged in the working buffer
   row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.W, w.ld, n, w.dr);
   UPDES_LAUNCH_CHECK();
-  col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(w.W, w.ld, n, w.dr, w.dc);
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.dc, 0, size_t(n) * sizeof(double), s));
+  col_max_kernel<<<dim3(unsigned(ceil_div(n, 256)), kColScaleChunks), 256, 0, s>>>(
+      w.W, w.ld, n, w.dr, reinterpret_cast<unsigned long long*>(w.dc));
+  UPDES_LAUNCH_CHECK();
+  col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(n, w.dc);
   UPDES_LAUNCH_CHECK();
   split_df_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.W, w.ld, w.Khi, w.Klo, w.ld, n, w.dr,
                                                                              w.dc);
