@@ -312,8 +312,110 @@ def run_ours(args, world, rank, local):
         "kernel_ms_per_step": {k: v["ms"] / steps for k, v in per.items()},
         "cpu_baseline": cpu,
     }
+    if rank == 0 and not args.no_extra:
+        line["configs"] = extra_configs(args, U, torch)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def extra_configs(args, U, torch):
+    """The other benchmark configurations, each bounded to seconds, measured with CUDA events (device work)
+    on the current stream or the wall clock around a synchronised call (noted per entry)."""
+    from updes_gb300 import workloads as WL
+    from updes_gb300.multirhs import MultiRHSSolver
+    out = {}
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream()
+
+    # README Laplace, N = 600: latency of one solve through the public API (host arrays in and out)
+    sysd = WL.readme_laplace()
+    for prec in ("fp64", "fp32"):
+        o = U.SolverOptions(precision=prec, reuse_factorization=False)
+        for _ in range(3):
+            U.pde_solver_jit(options=o, **sysd)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 20
+        for _ in range(reps):
+            U.pde_solver_jit(options=o, **sysd)
+        torch.cuda.synchronize()
+        ms = 1000 * (time.perf_counter() - t0) / reps
+        out[f"readme_laplace_N600_{prec}"] = {"metric": "solves/s through pde_solver_jit (wall clock)",
+                                              "value": 1000.0 / ms, "ms_per_solve": ms}
+
+    # Advection-diffusion, N = 6,400, 64 bumps, 500 implicit steps captured in a CUDA graph
+    sysd, U0, dt = WL.advection_bumps(80, 64)
+    t0 = time.perf_counter()
+    solver = MultiRHSSolver(sysd["diff_operator"], sysd["cloud"], sysd["boundary_conditions"], sysd["rbf"],
+                            sysd["max_degree"], sweeps=1)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    Ud = torch.as_tensor(U0, device="cuda").contiguous()
+    g = solver.make_graph(Ud, steps_per_graph=1, rhs_scale=1.0 / dt)
+    for _ in range(3):
+        g.replay()
+    steps = args.adv_steps
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(steps):
+        g.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    solver.check_status()
+    ms = e0.elapsed_time(e1) / steps
+    out["advection_diffusion_N6400_R64"] = {
+        "metric": "column-solves/s (64 right-hand sides per implicit step, graph replay, CUDA events)",
+        "value": 64 * 1000.0 / ms, "ms_per_step": ms, "steps": steps, "factor_setup_s": setup_s,
+        "factors": "FP64, applied as double-float planes, one refinement sweep"}
+
+    # Boundary control with adjoint, N = 10,000, r^5, FP64: forward and reverse through the solve
+    from updes_gb300.adjoint import pde_solver_torch
+    sysd, F, controls, ut = WL.boundary_control(100, 32)
+    cl = sysd["cloud"]
+    Ni = cl.Ni
+    utd = torch.as_tensor(ut, device="cuda")
+    o = U.SolverOptions(precision="fp64")
+    fwd_ms, bwd_ms = [], []
+    for i in range(4):
+        ctl = torch.tensor(controls[i], device="cuda", requires_grad=True)
+        ft = [torch.tensor(f, device="cuda", requires_grad=True) for f in F]
+        bcs = dict(sysd["boundary_conditions"])
+        bcs["North"] = ctl
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vals, _ = pde_solver_torch(sysd["diff_operator"], sysd["rhs_operator"], cl, bcs, sysd["rbf"],
+                                   sysd["max_degree"], diff_args=ft, options=o)
+        J = torch.mean((vals[:Ni] - utd[:Ni]) ** 2) + 1e-4 * torch.sum(ctl ** 2)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        J.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if i > 0:  # the first pair warms up
+            fwd_ms.append(1000 * (t1 - t0))
+            bwd_ms.append(1000 * (t2 - t1))
+    f, b = statistics.median(fwd_ms), statistics.median(bwd_ms)
+    out["boundary_control_adjoint_N10000"] = {
+        "metric": "gradient evaluations/s (forward + reverse, wall clock, host capture included)",
+        "value": 1000.0 / (f + b), "forward_ms": f, "backward_ms": b, "backward_over_forward": b / f}
+
+    # Batched uneven clouds: 512 independent systems, 8 streams
+    systems = WL.uneven_clouds(args.batch_count)
+    for prec in ("fp32", "fp64"):
+        o = U.SolverOptions(precision=prec, reuse_factorization=False)
+        U.pde_solver_many(systems[:16], options=o, streams=8)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        U.pde_solver_many(systems, options=o, streams=8)
+        torch.cuda.synchronize()
+        dt_s = time.perf_counter() - t0
+        infos = U.operators.LAST_MANY_INFO
+        out[f"uneven_clouds_{len(systems)}_{prec}"] = {
+            "metric": "systems/s through pde_solver_many (wall clock, host preparation included)",
+            "value": len(systems) / dt_s, "seconds": dt_s,
+            "fell_back": int(sum(i["fell_back"] for i in infos)),
+            "converged": int(sum(i["converged"] for i in infos))}
+    return out
 
 
 class _Null:
@@ -335,6 +437,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--sample-nx", type=int, default=70)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
+    ap.add_argument("--adv-steps", type=int, default=500)
+    ap.add_argument("--batch-count", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -282,6 +282,24 @@ UPDES_API int updes_workspace_status(const updes_problem* p, void* workspace, si
 UPDES_API int updes_eval_values_batch(const updes_problem* p, int32_t R, const double* C, int64_t ldc, double* vals,
                                       int64_t ldv, void* stream);
 
+/*
+ * Many independent systems in one call: problems[i] (its own cloud, kernel and
+ * boundary rows) with rhs q[i] (N_i) gives coeffs[i] (n_i) and, when vals is
+ * non-null and vals[i] non-null, vals[i] (N_i); infos (may be null) receives
+ * each solve's report.  `streams` (1..64) host threads each drive one CUDA
+ * stream with its own workspace slice and take the next unsolved system,
+ * largest first; every solve is updes_solve.  The call returns when all are
+ * done, with the first nonzero status it met (the others still ran).
+ * workspace: updes_solve_many_workspace bytes (the largest system's solve
+ * workspace per stream).  The reference runs one pde_solver call per system
+ * (updes/operators.py:559-618).
+ */
+UPDES_API int updes_solve_many_workspace(const updes_problem* problems, int32_t count, const updes_solve_opts* opts,
+                                         int32_t streams, size_t* bytes);
+UPDES_API int updes_solve_many(const updes_problem* problems, int32_t count, const double* const* q,
+                               double* const* coeffs, double* const* vals, const updes_solve_opts* opts,
+                               updes_solve_info* infos, void* workspace, size_t workspace_bytes, int32_t streams);
+
 /* ---- adjoint (reverse mode through the solve) ------------------------------
  * The reference differentiates pde_solver with jax.grad through inv, the GEMM
  * and the lineax QR (demos/Laplace/10_laplace_with_diff_phys.py:89-104) or runs

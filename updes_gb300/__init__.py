@@ -10,7 +10,7 @@ from .operators import (
     DEFAULT_OPTIONS, LAST_INFO, CollocationMatrix, SolverOptions, SteadySol, boundary_conditions_func_to_arr,
     capture_operator, compute_coefficients, compute_nb_monomials, core_compute_coefficients, divergence,
     get_field_coefficients, gradient, gradient_vec, laplacian, laplacian_vec, make_all_monomials, make_monomial,
-    nodal_div_grad, nodal_gradient, nodal_laplacian, nodal_value, pde_solver, pde_solver_jit,
+    nodal_div_grad, nodal_gradient, nodal_laplacian, nodal_value, pde_solver, pde_solver_jit, pde_solver_many,
     pde_solver_jit_with_bc, value, value_vec,
 )
 from .rbf import distance, gaussian, inverse_multiquadric, multiquadric, polyharmonic, rbf_spec, thin_plate

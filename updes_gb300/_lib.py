@@ -108,6 +108,10 @@ SIGNATURES = {
                                          _sz, _vp]),
     "updes_workspace_status": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _sz, ctypes.POINTER(_i32), _vp]),
     "updes_eval_values_batch": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _i64, _vp, _i64, _vp]),
+    "updes_solve_many_workspace": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, ctypes.POINTER(SolveOpts), _i32,
+                                                  ctypes.POINTER(_sz)]),
+    "updes_solve_many": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _vp, _vp, ctypes.POINTER(SolveOpts),
+                                        ctypes.POINTER(SolveInfo), _vp, _sz, _i32]),
     "updes_eval_values_t": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp]),
     "updes_solve_transpose": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),

@@ -20,6 +20,8 @@
 // accumulators in tensor memory); every wait is bounded.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "gemm_tc.cuh"
 #include "stats.cuh"
 
@@ -452,10 +454,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 int ozaki_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
                  int m, int nc, int K, DeviceStatus* st, cudaStream_t s) {
   if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};  // idempotent one-time set-up
+  if (!attr.load()) {
     UPDES_CUDA_TRY(cudaFuncSetAttribute(ozaki_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    attr = true;
+    attr.store(true);
   }
   dim3 grid(unsigned(ceil_div(nc, TN)), unsigned(ceil_div(m, TM)));
   StatScope sc(kStatGemm, s, 2.0 * m * double(nc) * K, double(m) * nc * 16.0 + (double(m) + nc) * K * 4.0);

@@ -24,6 +24,8 @@
 // The fold of one k block runs while the tensor cores work on the next, and the C read-modify-write of a
 // tile overlaps the MMAs of the following tile.  Every mbarrier wait is bounded; a timeout sets the status
 // word and an abort flag that every role checks, and tensor memory is freed on every path.
+#include <atomic>
+
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -577,14 +579,14 @@ int make_map_c(CUtensorMap* map, float* base, int rows, int cols, int64_t ld) {
 }
 
 int num_sms_cached() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
+  static std::atomic<int> sms{0};
+  if (!sms.load()) {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    sms.store(v > 0 ? v : 1);
   }
-  return sms;
+  return sms.load();
 }
 
 }  // namespace
@@ -617,10 +619,10 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
   p += al(size_t(m) * nkb * 4);
   float* Bs = reinterpret_cast<float*>(p);
 
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};  // idempotent one-time set-up
+  if (!attr.load()) {
     UPDES_CUDA_TRY(cudaFuncSetAttribute(ozaki3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    attr = true;
+    attr.store(true);
   }
   CUtensorMap mapA, mapB, mapCh, mapCl;
   int e = make_map(&mapA, Ad, m, Kp, TM);

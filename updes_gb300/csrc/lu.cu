@@ -15,6 +15,8 @@
 #include <type_traits>
 #include <vector>
 
+#include <atomic>
+
 #include "common.cuh"
 #include "lu.cuh"
 #include "stats.cuh"
@@ -427,16 +429,16 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(double* W, int64_t ldw
   }
 }
 
-int g_num_sms = 0;
+std::atomic<int> g_num_sms{0};
 
 int num_sms() {
-  if (!g_num_sms) {
-    int dev = 0;
+  if (!g_num_sms.load()) {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 1;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    g_num_sms.store(v > 0 ? v : 1);
   }
-  return g_num_sms;
+  return g_num_sms.load();
 }
 
 }  // namespace
@@ -460,8 +462,9 @@ struct alignas(16) PanelRec {
   float row[kLuNb];
 };
 constexpr int kMaxPanelCtas = 32;
+constexpr int kPanelF32Threads = 512;  // 16 warps: the rank-1 update and the searches split over more rows
 
-__global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int64_t ld, int n, int k, int nb,
+__global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, int64_t ld, int n, int k, int nb,
                                                                   int rows_per_cta, int32_t* __restrict__ piv,
                                                                   PanelRec* recs, int32_t* swap_map,
                                                                   DeviceStatus* st) {
@@ -475,14 +478,14 @@ __global__ void __launch_bounds__(kPanelThreads) panel_f32_kernel(float* W, int6
   float* pprev = prow + kLuNb;                                            // 64: the previous column's pivot row
   __shared__ float s_cval[kMaxPanelCtas];
   __shared__ int s_cidx[kMaxPanelCtas];
-  __shared__ float red_v[kPanelThreads / 32];
-  __shared__ int red_i[kPanelThreads / 32];
+  __shared__ float red_v[kPanelF32Threads / 32];
+  __shared__ int red_i[kPanelF32Threads / 32];
   __shared__ int s_best;  // local candidate (tile row) for the next column, -1 if none
 
   const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int rbase = k + g * rows_per_cta;
   const int rcount = max(0, min(rows_per_cta, n - rbase));
-  constexpr int kW = kPanelThreads / 32;
+  constexpr int kW = kPanelF32Threads / 32;
 
   for (int l = wid; l < rcount; l += kW)
     for (int c = lane; c < nb; c += 32) tile[int64_t(l) * ldt + c] = W[int64_t(rbase + l) * ld + k + c];
@@ -703,19 +706,19 @@ int launch_panel_f32(float* W, int64_t ld, int n, int k, int w, int32_t* piv, Pa
   const int rows = int(ceil_div(m, G));
   const size_t smem = (size_t(rows) * (w + 1) + size_t(kMaxPanelCtas + 3) * kLuNb) * sizeof(float);
   if (smem > 200 * 1024) return UPDES_ERR_UNSUPPORTED;
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};  // idempotent one-time set-up
+  if (!attr.load()) {
     UPDES_CUDA_TRY(cudaFuncSetAttribute(panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
+    attr.store(true);
   }
   int per_sm = 0;
-  UPDES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_f32_kernel, kPanelThreads, smem));
+  UPDES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_f32_kernel, kPanelF32Threads, smem));
   if (per_sm * num_sms() < G) return UPDES_ERR_UNSUPPORTED;
   int k_ = k, nb_ = w, rows_ = rows, n_ = n;
   int64_t ld_ = ld;
   void* args[] = {&W, &ld_, &n_, &k_, &nb_, &rows_, &piv, &recs, &swap_map, &st};
   StatScope sc(kStatPanel, s, double(m) * w * w, double(m) * w * 8.0);
-  UPDES_CUDA_TRY(cudaLaunchCooperativeKernel((void*)panel_f32_kernel, dim3(G), dim3(kPanelThreads), args, smem, s));
+  UPDES_CUDA_TRY(cudaLaunchCooperativeKernel((void*)panel_f32_kernel, dim3(G), dim3(kPanelF32Threads), args, smem, s));
   stats_count_launch(1);
   return UPDES_OK;
 }
@@ -813,11 +816,11 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     if (c1 <= c0) return UPDES_OK;
     StatScope sc(kStatTrsm, s, double(w) * w * (c1 - c0), double(w) * (c1 - c0) * 12.0);
     if (w == 64) {
-      static bool attr = false;
-      if (!attr) {
+      static std::atomic<bool> attr{false};  // idempotent one-time set-up
+      if (!attr.load()) {
         UPDES_CUDA_TRY(cudaFuncSetAttribute(trsm_df64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             int(sizeof(TrsmDfSmem))));
-        attr = true;
+        attr.store(true);
       }
       trsm_df64_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 256, sizeof(TrsmDfSmem), s>>>(Whi, Wlo, ld, k, c0, c1);
     } else {
@@ -1232,25 +1235,211 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
 
 }  // namespace
 
+// (h, l) += (a, b) across the 4 lanes of an aligned group (double-float, FP32 instructions)
+__device__ __forceinline__ void df_quad_sum(float& h, float& l) {
+#pragma unroll
+  for (int o = 1; o <= 2; o <<= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    const float s = __fadd_rn(h, oh);
+    const float bb = __fsub_rn(s, h);
+    float t = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(oh, bb));
+    t = __fadd_rn(t, __fadd_rn(l, ol));
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+  }
+}
+
+// Triangular solve with FP32 factors and inverted diagonal blocks (the refinement's preconditioner).
+// Same ticket/done-counter chain as trsv_kernel, arranged for a short critical path: four threads per row
+// (16 columns each, so every reduction is two shuffles), the block's right-hand side split into
+// double-float before the wait, and every solved block published twice, as FP64 x and as the double-float
+// planes xh/xl that the later blocks read (no FP64 conversions on the chain).
+template <int MODE>
+__global__ void __launch_bounds__(256) trsv_f32_kernel(const float* __restrict__ F, int64_t ldf, int n, double* x,
+                                                       float* xh_g, float* xl_g, int* ticket, int* flags,
+                                                       DeviceStatus* st, const float* __restrict__ dinv) {
+  __shared__ float sT[kTB][kTB + 1];
+  extern __shared__ __align__(16) unsigned char tf_smem[];
+  float(*sDh)[kTB + 1] = reinterpret_cast<float(*)[kTB + 1]>(tf_smem);
+  float(*sDl)[kTB + 1] = sDh + kTB;
+  __shared__ float sxh[kTB], sxl[kTB], srh[kTB], srl[kTB];
+  __shared__ int s_blk, s_done;
+  const int tid = threadIdx.x;
+  const int nblk = int(ceil_div(n, kTB));
+  if (tid == 0) {
+    s_blk = atomicAdd(ticket, 1);
+    s_done = 0;
+  }
+  __syncthreads();
+  const int t = s_blk;
+  if (t >= nblk) return;
+  constexpr bool fwd = (MODE == 0 || MODE == 2);
+  constexpr bool trans = (MODE >= 2);
+  const int blk = fwd ? t : nblk - 1 - t;
+  const int r0 = blk * kTB;
+  const int rows = min(kTB, n - r0);
+  const int row = tid >> 2, part = tid & 3;
+  // inputs no other block writes, fetched before any wait
+  float bh = 0.f, bl = 0.f;
+  if (part == 0 && row < rows) {
+    const double b = x[r0 + row];
+    bh = float(b);
+    bl = float(b - double(bh));
+  }
+  {
+    constexpr int which = (MODE == 0 || MODE == 3) ? 0 : 1;  // 0: inv(L_bb), 1: inv(U_bb); transposed for 2, 3
+    const float* Dh = dinv + (size_t(blk) * 4 + which * 2) * kTB * kTB;
+    const float* Dlo = Dh + kTB * kTB;
+    for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+      const int a = e >> 6, b = e & 63;
+      const int ra = trans ? b : a, cb = trans ? a : b;
+      sDh[ra][cb] = __ldg(Dh + e);
+      sDl[ra][cb] = __ldg(Dlo + e);
+    }
+  }
+  auto load_tile = [&](int c0, float (&pre)[16]) {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int e = tid + 256 * i;
+      const int a = e >> 6, b = e & 63;
+      float v = 0.f;
+      if (!trans) {
+        if (r0 + a < n && c0 + b < n) v = F[int64_t(r0 + a) * ldf + c0 + b];
+      } else {
+        if (c0 + a < n && r0 + b < n) v = F[int64_t(c0 + a) * ldf + r0 + b];
+      }
+      pre[i] = v;
+    }
+  };
+  float pre[16];
+  if (t > 0) load_tile((fwd ? 0 : nblk - 1) * kTB, pre);
+  float ah = 0.f, al = 0.f;
+  for (int q = 0; q < t; ++q) {
+    const int jb = fwd ? q : nblk - 1 - q;
+    const int c0 = jb * kTB;
+    const int cols = min(kTB, n - c0);
+    if (tid == 0 && s_done <= q) {
+      volatile int* vc = flags + nblk;
+      long long it = 0;
+      int d;
+      while ((d = *vc) <= q) {
+        if (++it > kSpinLimit) {
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, 20 + MODE);
+          d = q + 1;
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+      s_done = d;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int e = tid + 256 * i;
+      const int a = e >> 6, b = e & 63;
+      if (!trans) sT[a][b] = pre[i];
+      else sT[b][a] = pre[i];
+    }
+    if (tid < kTB) {
+      sxh[tid] = tid < cols ? __ldcg(xh_g + c0 + tid) : 0.f;
+      sxl[tid] = tid < cols ? __ldcg(xl_g + c0 + tid) : 0.f;
+    }
+    __syncthreads();
+    if (q + 1 < t) load_tile((fwd ? q + 1 : nblk - 2 - q) * kTB, pre);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const int c = part * 16 + ((k + 4 * part) & 15);  // rotated per part: fewer bank conflicts
+      df_fma(sT[row][c], sxh[c], sxl[c], ah, al);
+    }
+    __syncthreads();
+  }
+  df_quad_sum(ah, al);
+  if (part == 0) {
+    // right-hand side of this block minus the off-diagonal part, double-float
+    float rh = 0.f, rl = 0.f;
+    if (row < rows) {
+      const float ch = -ah, cl = -al;
+      const float s0 = __fadd_rn(bh, ch);
+      const float bb = __fsub_rn(s0, bh);
+      float tt = __fadd_rn(__fsub_rn(bh, __fsub_rn(s0, bb)), __fsub_rn(ch, bb));
+      tt = __fadd_rn(tt, __fadd_rn(bl, cl));
+      rh = __fadd_rn(s0, tt);
+      rl = __fsub_rn(tt, __fsub_rn(rh, s0));
+    }
+    srh[row] = rh;
+    srl[row] = rl;
+  }
+  __syncthreads();
+  // x_blk = D (b - off-diagonal part)
+  float ph = 0.f, pl = 0.f;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int c = part * 16 + ((k + 4 * part) & 15);
+    const float dh = sDh[row][c], dl = sDl[row][c], xh = srh[c], xl = srl[c];
+    const float p = __fmul_rn(dh, xh);
+    const float pe = __fmaf_rn(dh, xh, -p);
+    const float s0 = __fadd_rn(ph, p);
+    const float bb = __fsub_rn(s0, ph);
+    float tt = __fadd_rn(__fsub_rn(ph, __fsub_rn(s0, bb)), __fsub_rn(p, bb));
+    tt = __fadd_rn(tt, __fadd_rn(pl, __fmaf_rn(dh, xl, __fmaf_rn(dl, xh, pe))));
+    ph = __fadd_rn(s0, tt);
+    pl = __fsub_rn(tt, __fsub_rn(ph, s0));
+  }
+  df_quad_sum(ph, pl);
+  if (part == 0 && row < rows) {
+    xh_g[r0 + row] = ph;
+    xl_g[r0 + row] = pl;
+    x[r0 + row] = double(ph) + double(pl);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicAdd(flags + nblk, 1);  // blocks finish in order: this is block number t
+  }
+}
+
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
-              const float* dinv) {
+              const float* dinv, float* xh, float* xl) {
   const int nblk = int(ceil_div(n, kTB));
   StatScope sc(kStatTrsv, s, double(n) * n, double(n) * n * 0.5 * sizeof(TF));
   UPDES_CUDA_TRY(cudaMemsetAsync(sync_ws, 0, sizeof(int) * (nblk + 2), s));
   int* ticket = sync_ws;
   int* flags = sync_ws + 1;
   if (sizeof(TF) != 4) dinv = nullptr;
+  if constexpr (sizeof(TF) == 4) {
+    if (dinv && xh && xl) {
+      const size_t smem = 2 * sizeof(float) * kTB * (kTB + 1);
+      static std::atomic<bool> attr{false};  // idempotent one-time set-up
+      if (!attr.load()) {
+        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        attr.store(true);
+      }
+      switch (mode) {
+        case 0: trsv_f32_kernel<0><<<nblk, 256, smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+        case 1: trsv_f32_kernel<1><<<nblk, 256, smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+        case 2: trsv_f32_kernel<2><<<nblk, 256, smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+        default: trsv_f32_kernel<3><<<nblk, 256, smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+      }
+      UPDES_LAUNCH_CHECK();
+      return UPDES_OK;
+    }
+  }
   const size_t smem =
       sizeof(TF) * kTB * (kTB + 1) + kTB * (8 + 4 + 4 + 8) + (dinv ? 2 * sizeof(float) * kTB * (kTB + 1) : 0);
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};  // idempotent one-time set-up
+  if (!attr.load()) {
     const int big = int(sizeof(TF) * kTB * (kTB + 1) + kTB * 24 + 2 * sizeof(float) * kTB * (kTB + 1));
     UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    attr = true;
+    attr.store(true);
   }
   switch (mode) {
     case 0: trsv_kernel<TF, 0><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st, dinv); break;
@@ -1263,9 +1452,9 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
 }
 
 template int trsv_impl<double>(int, const double*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
-                               const float*);
+                               const float*, float*, float*);
 template int trsv_impl<float>(int, const float*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
-                              const float*);
+                              const float*, float*, float*);
 
 namespace {
 
@@ -1322,10 +1511,10 @@ size_t diag_inverse_bytes(int n) { return size_t(ceil_div(n, kTB)) * 4 * kTB * k
 
 int diag_inverse(int n, const float* F, int64_t ldf, float* dinv, cudaStream_t s) {
   const size_t smem = 3 * kTB * (kTB + 1) * sizeof(double);
-  static bool attr = false;
-  if (!attr) {
+  static std::atomic<bool> attr{false};  // idempotent one-time set-up
+  if (!attr.load()) {
     UPDES_CUDA_TRY(cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    attr = true;
+    attr.store(true);
   }
   StatScope sc(kStatOther, s, 2.0 * kTB * kTB * kTB / 3.0 * ceil_div(n, kTB), diag_inverse_bytes(n));
   diag_inverse_kernel<<<unsigned(ceil_div(n, kTB)), 128, smem, s>>>(F, ldf, n, dinv);

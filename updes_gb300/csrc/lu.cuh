@@ -20,9 +20,11 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
 // mode: 0 = L, 1 = U, 2 = U^T, 3 = L^T (x overwritten in place); sync_ws: ceil(n/64)+1 ints.
 // dinv (FP32 factors only, may be null): inverted diagonal blocks from diag_inverse, applied as matvecs
 // instead of the substitution inside each block.
+// xh, xl (n FP32 each, may be null): scratch planes that carry solved blocks in double-float between CTAs
+// (used together with dinv).
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
-              const float* dinv = nullptr);
+              const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr);
 
 // Inverses of the 64 x 64 diagonal blocks of FP32 LU factors, as double-float planes (diag_inverse_bytes).
 size_t diag_inverse_bytes(int n);

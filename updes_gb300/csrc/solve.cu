@@ -475,22 +475,22 @@ int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t l
 // x (contiguous, n) <- A^-1 x or A^-T x using the permutation in piv[n, 2n)
 template <typename TF>
 int solve_core(int n, const TF* F, int64_t ldf, const int32_t* piv, double* x, int trans, const LuWs& w,
-               cudaStream_t s, const float* dinv = nullptr) {
+               cudaStream_t s, const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr) {
   const int32_t* perm = piv + n;
   const unsigned g = unsigned(ceil_div(n, 256));
   if (!trans) {
     permute_kernel<<<g, 256, 0, s>>>(w.tmp, x, 1, 1, perm, n, 0);
     UPDES_LAUNCH_CHECK();
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv, xh, xl);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv, xh, xl);
     if (e) return e;
     UPDES_CUDA_TRY(cudaMemcpyAsync(x, w.tmp, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
   } else {
     UPDES_CUDA_TRY(cudaMemcpyAsync(w.tmp, x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv, xh, xl);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv, xh, xl);
     if (e) return e;
     permute_kernel<<<g, 256, 0, s>>>(x, w.tmp, 1, 1, perm, n, 1);
     UPDES_LAUNCH_CHECK();
@@ -725,7 +725,7 @@ int residual_scaled(const SolveWs& w, int n, const double* x, double* out, doubl
 
 int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s, bool trans = false) {
   if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
-  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv);
+  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv, w.xh, w.xl);
 }
 
 [[maybe_unused]] double host_norm(const std::vector<double>& v) {

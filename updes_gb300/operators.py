@@ -738,3 +738,57 @@ def materialize_B(dp, cloud, rbf, max_degree):
     _lib.check(lib.updes_lu_solve(n, A.data_ptr(), ld, _lib.PREC_FP64, piv.data_ptr(), Y.data_ptr(), N, N, 1,
                                   ws.data_ptr(), ws.numel(), dp.stream()), "updes_lu_solve")
     return Y.T[:, :N].cpu().numpy().copy()
+
+
+def pde_solver_many(systems, options=None, streams=8):
+    """Solve many independent systems in one call (``updes_solve_many``).
+
+    ``systems``: a sequence of dicts with the keyword arguments of ``pde_solver``
+    (``diff_operator``, ``rhs_operator``, ``cloud``, ``boundary_conditions``,
+    ``rbf``, ``max_degree`` and optionally ``diff_args``, ``rhs_args``); callable
+    boundary conditions are evaluated as in ``pde_solver_jit``.  Returns a list of
+    ``SteadySol`` in the same order.  The solves run on ``streams`` CUDA streams
+    at once, largest system first; each is exactly ``pde_solver``'s solve.
+    """
+    torch = _torch()
+    lib = _lib.load()
+    opts = options or DEFAULT_OPTIONS
+    dps, qs = [], []
+    for sysd in systems:
+        cloud = sysd["cloud"]
+        bcs = boundary_conditions_func_to_arr(sysd["boundary_conditions"], cloud)
+        W, kind, bnodes, geom, q = prepare(sysd["diff_operator"], sysd["rhs_operator"], cloud, bcs, sysd["rbf"],
+                                           sysd["max_degree"], sysd.get("diff_args"), sysd.get("rhs_args"), opts)
+        dp = DeviceProblem(cloud, sysd["rbf"], sysd["max_degree"], W, kind, bnodes, geom, opts.self_term)
+        dps.append(dp)
+        qs.append(torch.as_tensor(q, dtype=torch.float64, device=dp.device))
+    count = len(dps)
+    if count == 0:
+        return []
+    coeffs = [torch.empty(dp.n, dtype=torch.float64, device=dp.device) for dp in dps]
+    vals = [torch.empty(dp.N, dtype=torch.float64, device=dp.device) for dp in dps]
+    probs = (_lib.Problem * count)(*[dp.c for dp in dps])
+    ptrs = lambda ts: (ctypes.c_void_p * count)(*[t.data_ptr() for t in ts])
+    qp, cp, vp = ptrs(qs), ptrs(coeffs), ptrs(vals)
+    infos = (_lib.SolveInfo * count)()
+    co = opts.c_opts()
+    nbytes = ctypes.c_size_t()
+    _lib.check(lib.updes_solve_many_workspace(probs, count, ctypes.byref(co), int(streams), ctypes.byref(nbytes)),
+               "updes_solve_many_workspace")
+    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=dps[0].device)
+    torch.cuda.synchronize()  # the library's streams do not order with the caller's
+    st = lib.updes_solve_many(probs, count, ctypes.cast(qp, ctypes.c_void_p), ctypes.cast(cp, ctypes.c_void_p),
+                              ctypes.cast(vp, ctypes.c_void_p), ctypes.byref(co), infos, ws.data_ptr(), ws.numel(),
+                              int(streams))
+    LAST_MANY_INFO[:] = [infos[i].as_dict() for i in range(count)]
+    _lib.check(st, "updes_solve_many")
+    out = []
+    for sysd, dp, c, v in zip(systems, dps, coeffs, vals):
+        cloud, rbf, deg = sysd["cloud"], sysd["rbf"], sysd["max_degree"]
+        out.append(SteadySol(v.cpu().numpy(), c.cpu().numpy(),
+                             CollocationMatrix(lambda dp=dp, cloud=cloud, rbf=rbf, deg=deg:
+                                               materialize_B(dp, cloud, rbf, deg))))
+    return out
+
+
+LAST_MANY_INFO: list = []
