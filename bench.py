@@ -320,14 +320,22 @@ def run_ours(args, world, rank, local):
 
 def extra_configs(args, U, torch):
     """The other benchmark configurations, each bounded to seconds, measured with CUDA events (device work)
-    on the current stream or the wall clock around a synchronised call (noted per entry)."""
-    from updes_gb300 import workloads as WL
-    from updes_gb300.multirhs import MultiRHSSolver
+    on the current stream or the wall clock around a synchronised call (noted per entry).  A configuration
+    that fails records its error and the others still run."""
     out = {}
-    ev = lambda: torch.cuda.Event(enable_timing=True)
-    stream = torch.cuda.current_stream()
+    for fn in (_cfg_readme, _cfg_advection, _cfg_control, _cfg_uneven):
+        try:
+            out.update(fn(args, U, torch))
+        except Exception as e:  # noqa: BLE001 - reported in the JSON line
+            torch.cuda.synchronize()
+            out[fn.__name__[5:]] = {"error": f"{type(e).__name__}: {e}"}
+    return out
 
-    # README Laplace, N = 600: latency of one solve through the public API (host arrays in and out)
+
+def _cfg_readme(args, U, torch):
+    """README Laplace, N = 600: latency of one solve through the public API (host arrays in and out)."""
+    from updes_gb300 import workloads as WL
+    out = {}
     sysd = WL.readme_laplace()
     for prec in ("fp64", "fp32"):
         o = U.SolverOptions(precision=prec, reuse_factorization=False)
@@ -342,8 +350,14 @@ def extra_configs(args, U, torch):
         ms = 1000 * (time.perf_counter() - t0) / reps
         out[f"readme_laplace_N600_{prec}"] = {"metric": "solves/s through pde_solver_jit (wall clock)",
                                               "value": 1000.0 / ms, "ms_per_solve": ms}
+    return out
 
-    # Advection-diffusion, N = 6,400, 64 bumps, 500 implicit steps captured in a CUDA graph
+
+def _cfg_advection(args, U, torch):
+    """Advection-diffusion, N = 6,400, 64 bumps, implicit steps replayed from a CUDA graph."""
+    from updes_gb300 import workloads as WL
+    from updes_gb300.multirhs import MultiRHSSolver
+    stream = torch.cuda.current_stream()
     sysd, U0, dt = WL.advection_bumps(80, 64)
     t0 = time.perf_counter()
     solver = MultiRHSSolver(sysd["diff_operator"], sysd["cloud"], sysd["boundary_conditions"], sysd["rbf"],
@@ -355,7 +369,7 @@ def extra_configs(args, U, torch):
     for _ in range(3):
         g.replay()
     steps = args.adv_steps
-    e0, e1 = ev(), ev()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(steps):
         g.replay()
@@ -363,12 +377,15 @@ def extra_configs(args, U, torch):
     torch.cuda.synchronize()
     solver.check_status()
     ms = e0.elapsed_time(e1) / steps
-    out["advection_diffusion_N6400_R64"] = {
+    return {"advection_diffusion_N6400_R64": {
         "metric": "column-solves/s (64 right-hand sides per implicit step, graph replay, CUDA events)",
         "value": 64 * 1000.0 / ms, "ms_per_step": ms, "steps": steps, "factor_setup_s": setup_s,
-        "factors": "FP64, applied as double-float planes, one refinement sweep"}
+        "factors": "FP64, applied as double-float planes, one refinement sweep"}}
 
-    # Boundary control with adjoint, N = 10,000, r^5, FP64: forward and reverse through the solve
+
+def _cfg_control(args, U, torch):
+    """Boundary control with adjoint, N = 10,000, r^5, FP64: forward and reverse through the solve."""
+    from updes_gb300 import workloads as WL
     from updes_gb300.adjoint import pde_solver_torch
     sysd, F, controls, ut = WL.boundary_control(100, 32)
     cl = sysd["cloud"]
@@ -395,11 +412,15 @@ def extra_configs(args, U, torch):
             fwd_ms.append(1000 * (t1 - t0))
             bwd_ms.append(1000 * (t2 - t1))
     f, b = statistics.median(fwd_ms), statistics.median(bwd_ms)
-    out["boundary_control_adjoint_N10000"] = {
+    return {"boundary_control_adjoint_N10000": {
         "metric": "gradient evaluations/s (forward + reverse, wall clock, host capture included)",
-        "value": 1000.0 / (f + b), "forward_ms": f, "backward_ms": b, "backward_over_forward": b / f}
+        "value": 1000.0 / (f + b), "forward_ms": f, "backward_ms": b, "backward_over_forward": b / f}}
 
-    # Batched uneven clouds: 512 independent systems, 8 streams
+
+def _cfg_uneven(args, U, torch):
+    """Batched uneven clouds: independent systems of 100 to 2,025 nodes on 8 streams."""
+    from updes_gb300 import workloads as WL
+    out = {}
     systems = WL.uneven_clouds(args.batch_count)
     for prec in ("fp32", "fp64"):
         o = U.SolverOptions(precision=prec, reuse_factorization=False)

@@ -44,3 +44,23 @@ def test_many_rejects_bad_arguments():
     nb = ctypes.c_size_t()
     assert lib.updes_solve_many_workspace(None, 1, None, 1, ctypes.byref(nb)) == _lib.ERR_INVALID
     assert lib.updes_solve_many(None, 0, None, None, None, None, None, None, 0, 1) == _lib.ERR_INVALID
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_many_uneven_clouds(precision):
+    """Uneven clouds (100 to 2,025 nodes; Gaussian and r^5 kernels; Dirichlet, Neumann and Robin facets) on
+    8 streams: systems of different sizes factor at the same time, a second call repeats the first bitwise,
+    and each result is bitwise the system solved alone."""
+    from updes_gb300 import workloads as WL
+    systems = WL.uneven_clouds(24, seed=3)
+    opts = U.SolverOptions(precision=precision, reuse_factorization=False)
+    first = U.pde_solver_many(systems, options=opts, streams=8)
+    many = U.pde_solver_many(systems, options=opts, streams=8)
+    infos = U.operators.LAST_MANY_INFO
+    assert all(i["converged"] == 1 for i in infos)
+    for a, b in zip(first, many):
+        assert np.array_equal(a.vals, b.vals)
+    for k in (0, 1, 7, 23):
+        one = U.pde_solver_jit(options=opts, **systems[k])
+        assert np.array_equal(many[k].vals, one.vals)
+        assert np.array_equal(many[k].coeffs, one.coeffs)

@@ -372,14 +372,7 @@ size_t batch_layout(int n, char* base, BatchWs* w) {
 // host call that is not a stream operation, made before the first launch).
 int batch_kernel_setup() {
   static std::atomic<unsigned long long> ready{0};
-  int dev = 0;
-  UPDES_CUDA_TRY(cudaGetDevice(&dev));
-  const unsigned long long bit = 1ull << (dev & 63);
-  if (ready.load() & bit) return UPDES_OK;
-  UPDES_CUDA_TRY(cudaFuncSetAttribute(batch_kx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(sizeof(KxSmem))));
-  ready.fetch_or(bit);
-  return UPDES_OK;
+  return smem_opt_in((const void*)batch_kx_kernel, int(sizeof(KxSmem)), ready);
 }
 
 }  // namespace

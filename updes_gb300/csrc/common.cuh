@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/updes_gb300.h"
 
 #define UPDES_CUDA_TRY(expr)                                   \
@@ -22,8 +24,24 @@ void stats_count_launch(int n);
     UPDES_CUDA_TRY(cudaGetLastError()); \
   } while (0)
 
-// Records the last CUDA error (text retrievable through updes_last_error()).
+// Records the last CUDA error (text retrievable through updes_last_error()) and clears the calling
+// thread's pending runtime error, so that a failure reported once is not reported again by the next
+// launch check of an unrelated call on the same thread.
 void updes_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the current device, once per device
+// (`done` holds one bit per device ordinal).  The limit belongs to the function on the device and is
+// shared by every host thread, so it is set to the kernel's largest need and never changed per call: a
+// per-call value set by one thread could undercut a launch that another thread is about to make.
+inline int smem_opt_in(const void* func, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  UPDES_CUDA_TRY(cudaGetDevice(&dev));
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load() & bit) return UPDES_OK;
+  UPDES_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done.fetch_or(bit);
+  return UPDES_OK;
+}
 
 // Device-side status word layout (written by kernels, read by the host after a sync).
 // word 0: first error code (UPDES_ERR_*) raised by any kernel, 0 if none

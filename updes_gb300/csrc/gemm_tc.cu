@@ -454,11 +454,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 int ozaki_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
                  int m, int nc, int K, DeviceStatus* st, cudaStream_t s) {
   if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
-  static std::atomic<bool> attr{false};  // idempotent one-time set-up
-  if (!attr.load()) {
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(ozaki_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    attr.store(true);
-  }
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)ozaki_update_kernel, kSmemBytes, attr)) return e;
   dim3 grid(unsigned(ceil_div(nc, TN)), unsigned(ceil_div(m, TM)));
   StatScope sc(kStatGemm, s, 2.0 * m * double(nc) * K, double(m) * nc * 16.0 + (double(m) + nc) * K * 4.0);
   ozaki_update_kernel<<<grid, kThreads, kSmemBytes, s>>>(Chi, Clo, ldc, A, lda, B, ldb, m, nc, K, st);

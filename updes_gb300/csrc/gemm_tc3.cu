@@ -37,7 +37,10 @@ namespace {
 constexpr int TM = 128, TN = 64, TK = 64;
 constexpr int kDigits = 3, kGroups = 4;  // 8 digit products
 constexpr int kStages = 2;
-constexpr int kWarps = 10, kThreads = kWarps * 32, kEpiWarps = 8;
+// epilogue: kEpiWarps warps, four per lane quarter of the tile (the warps a TMEM lane quarter allows), each
+// with kEpiCols columns
+constexpr int kEpiWarps = 16, kEpiCols = TN / (kEpiWarps / 4);
+constexpr int kWarps = 2 + kEpiWarps, kThreads = kWarps * 32;
 constexpr uint32_t kTmemCols = 512;  // 2 sets x 4 groups x 64 columns
 constexpr int kATile = TM * TK * 2;  // 16 KB per digit plane
 constexpr int kBTile = TN * TK * 2;  //  8 KB per digit plane
@@ -399,19 +402,19 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // ---------------- epilogue: 8 warps, lane quarter q = warp % 4, column half h ----------------
+    // ---------------- epilogue: lane quarter q = warp % 4, column group h ----------------
     const int q = warp & 3, h = (warp - 2) >> 2;
     const int row_in_tile = q * 32 + lane;
-    const int colbase = h * 32;
+    const int colbase = h * kEpiCols;
     const uint32_t lane_base = uint32_t(q * 32) << 16;
     int j = 0, tl = 0;
     const bool storer = (warp == 2 && lane == 0);  // issues the C stores and frees the C buffer
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
       const int r0 = (t / tiles_n) * TM, c0 = (t % tiles_n) * TN;
       const int gr = r0 + row_in_tile;
-      float acc_h[32], acc_l[32];
+      float acc_h[kEpiCols], acc_l[kEpiCols];
 #pragma unroll
-      for (int u = 0; u < 32; ++u) { acc_h[u] = 0.f; acc_l[u] = 0.f; }
+      for (int u = 0; u < kEpiCols; ++u) { acc_h[u] = 0.f; acc_l[u] = 0.f; }
       bool ok = true;
       for (int kb = 0; kb < nkb; ++kb, ++j) {
         const int set = j & 1;
@@ -419,7 +422,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // scales of this k block (loaded before the wait): the row's, and one column's per lane
         const float sa = gr < m ? __ldg(As + int64_t(gr) * nkb + kb) : 0.f;
         const int my_c = c0 + colbase + lane;
-        const float my_sb = my_c < nc ? __ldg(Bs + int64_t(my_c) * nkb + kb) : 0.f;
+        const float my_sb = (lane < kEpiCols && my_c < nc) ? __ldg(Bs + int64_t(my_c) * nkb + kb) : 0.f;
         // every wait ends in a warp vote, so a warp always leaves together (tcgen05.ld needs all 32 lanes)
         if (!__all_sync(0xffffffffu, mbar_wait(&ctl.tfull[set], tph, abort_flag))) {
           if (lane == 0 && !*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 43); }
@@ -429,14 +432,14 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
 #pragma unroll
-        for (int ch = 0; ch < 4; ++ch) {
+        for (int ch = 0; ch < kEpiCols / 8; ++ch) {
           const int col = colbase + ch * 8;
           float g[kGroups][8];
 #pragma unroll
           for (int gi = 0; gi < kGroups; ++gi)
             tmem_ld8(tmem + lane_base + uint32_t(set * kGroups * TN + gi * TN + col), g[gi]);
           tmem_wait_ld();
-          if (ch == 3) {
+          if (ch == kEpiCols / 8 - 1) {
             // every chunk has been read: release the accumulator set to the MMA issuer
             tc_fence_before();
             __syncwarp();
@@ -472,11 +475,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       {
         // this thread's row in the 128B-swizzled boxes: 16-byte chunk q of row r sits at chunk q ^ (r & 7)
         const int r = row_in_tile;
-        uint8_t* hrow = sC + h * kCHalf + (r >> 3) * 1024 + (r & 7) * 128;
+        const int half = colbase >> 5, qbase = (colbase & 31) >> 2;  // box and first 16-byte chunk
+        uint8_t* hrow = sC + half * kCHalf + (r >> 3) * 1024 + (r & 7) * 128;
         uint8_t* lrow = hrow + 2 * kCHalf;
 #pragma unroll
-        for (int qq = 0; qq < 8; ++qq) {
-          const int off = ((qq ^ (r & 7)) << 4);
+        for (int qq = 0; qq < kEpiCols / 4; ++qq) {
+          const int off = (((qbase + qq) ^ (r & 7)) << 4);
           float4 hv = *reinterpret_cast<float4*>(hrow + off), lv = *reinterpret_cast<float4*>(lrow + off);
           float hx[4] = {hv.x, hv.y, hv.z, hv.w}, lx[4] = {lv.x, lv.y, lv.z, lv.w};
 #pragma unroll
@@ -619,11 +623,8 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
   p += al(size_t(m) * nkb * 4);
   float* Bs = reinterpret_cast<float*>(p);
 
-  static std::atomic<bool> attr{false};  // idempotent one-time set-up
-  if (!attr.load()) {
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(ozaki3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-    attr.store(true);
-  }
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)ozaki3_kernel, kSmemBytes, attr)) return e;
   CUtensorMap mapA, mapB, mapCh, mapCl;
   int e = make_map(&mapA, Ad, m, Kp, TM);
   if (e) return e;

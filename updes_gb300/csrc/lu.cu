@@ -706,11 +706,8 @@ int launch_panel_f32(float* W, int64_t ld, int n, int k, int w, int32_t* piv, Pa
   const int rows = int(ceil_div(m, G));
   const size_t smem = (size_t(rows) * (w + 1) + size_t(kMaxPanelCtas + 3) * kLuNb) * sizeof(float);
   if (smem > 200 * 1024) return UPDES_ERR_UNSUPPORTED;
-  static std::atomic<bool> attr{false};  // idempotent one-time set-up
-  if (!attr.load()) {
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(panel_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr.store(true);
-  }
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)panel_f32_kernel, 200 * 1024, attr)) return e;
   int per_sm = 0;
   UPDES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_f32_kernel, kPanelF32Threads, smem));
   if (per_sm * num_sms() < G) return UPDES_ERR_UNSUPPORTED;
@@ -746,7 +743,8 @@ int launch_panel(void* W, const float* Wlo, int64_t ldw, TF* F, int64_t ldf, int
   }
   if (smem > 200 * 1024) return UPDES_ERR_UNSUPPORTED;
   auto kern = panel_kernel<TF, DF_IN>;
-  UPDES_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)kern, 200 * 1024, attr)) return e;
   int per_sm = 0;
   UPDES_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPanelThreads, smem));
   if (per_sm * sms < G) return UPDES_ERR_UNSUPPORTED;
@@ -816,12 +814,8 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     if (c1 <= c0) return UPDES_OK;
     StatScope sc(kStatTrsm, s, double(w) * w * (c1 - c0), double(w) * (c1 - c0) * 12.0);
     if (w == 64) {
-      static std::atomic<bool> attr{false};  // idempotent one-time set-up
-      if (!attr.load()) {
-        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsm_df64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            int(sizeof(TrsmDfSmem))));
-        attr.store(true);
-      }
+      static std::atomic<unsigned long long> attr{0};
+      if (int e = smem_opt_in((const void*)trsm_df64_kernel, int(sizeof(TrsmDfSmem)), attr)) return e;
       trsm_df64_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 256, sizeof(TrsmDfSmem), s>>>(Whi, Wlo, ld, k, c0, c1);
     } else {
       trsm_df_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 64, 0, s>>>(Whi, Wlo, ld, k, w, c0, c1);
@@ -1412,14 +1406,13 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
   if constexpr (sizeof(TF) == 4) {
     if (dinv && xh && xl) {
       const size_t smem = 2 * sizeof(float) * kTB * (kTB + 1);
-      static std::atomic<bool> attr{false};  // idempotent one-time set-up
-      if (!attr.load()) {
-        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_f32_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-        attr.store(true);
-      }
+      static std::atomic<unsigned long long> attr[4] = {};
+      int e;
+      if ((e = smem_opt_in((const void*)trsv_f32_kernel<0>, int(smem), attr[0])) ||
+          (e = smem_opt_in((const void*)trsv_f32_kernel<1>, int(smem), attr[1])) ||
+          (e = smem_opt_in((const void*)trsv_f32_kernel<2>, int(smem), attr[2])) ||
+          (e = smem_opt_in((const void*)trsv_f32_kernel<3>, int(smem), attr[3])))
+        return e;
       switch (mode) {
         case 0: trsv_f32_kernel<0><<<nblk, 256, smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
         case 1: trsv_f32_kernel<1><<<nblk, 256, smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
@@ -1432,14 +1425,15 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
   }
   const size_t smem =
       sizeof(TF) * kTB * (kTB + 1) + kTB * (8 + 4 + 4 + 8) + (dinv ? 2 * sizeof(float) * kTB * (kTB + 1) : 0);
-  static std::atomic<bool> attr{false};  // idempotent one-time set-up
-  if (!attr.load()) {
+  {
     const int big = int(sizeof(TF) * kTB * (kTB + 1) + kTB * 24 + 2 * sizeof(float) * kTB * (kTB + 1));
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(trsv_kernel<TF, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    attr.store(true);
+    static std::atomic<unsigned long long> attr[4] = {};
+    int e;
+    if ((e = smem_opt_in((const void*)trsv_kernel<TF, 0>, big, attr[0])) ||
+        (e = smem_opt_in((const void*)trsv_kernel<TF, 1>, big, attr[1])) ||
+        (e = smem_opt_in((const void*)trsv_kernel<TF, 2>, big, attr[2])) ||
+        (e = smem_opt_in((const void*)trsv_kernel<TF, 3>, big, attr[3])))
+      return e;
   }
   switch (mode) {
     case 0: trsv_kernel<TF, 0><<<nblk, 256, smem, s>>>(F, ldf, n, x, ticket, flags, st, dinv); break;
@@ -1511,11 +1505,8 @@ size_t diag_inverse_bytes(int n) { return size_t(ceil_div(n, kTB)) * 4 * kTB * k
 
 int diag_inverse(int n, const float* F, int64_t ldf, float* dinv, cudaStream_t s) {
   const size_t smem = 3 * kTB * (kTB + 1) * sizeof(double);
-  static std::atomic<bool> attr{false};  // idempotent one-time set-up
-  if (!attr.load()) {
-    UPDES_CUDA_TRY(cudaFuncSetAttribute(diag_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    attr.store(true);
-  }
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)diag_inverse_kernel, int(smem), attr)) return e;
   StatScope sc(kStatOther, s, 2.0 * kTB * kTB * kTB / 3.0 * ceil_div(n, kTB), diag_inverse_bytes(n));
   diag_inverse_kernel<<<unsigned(ceil_div(n, kTB)), 128, smem, s>>>(F, ldf, n, dinv);
   UPDES_LAUNCH_CHECK();

@@ -8,10 +8,14 @@
 #include <algorithm>
 #include <atomic>
 #include <numeric>
+#include <string>
 #include <thread>
 #include <vector>
 
 #include "common.cuh"
+
+void updes_set_last_error_text(const std::string& text);
+std::string updes_last_error_text();
 
 namespace {
 
@@ -71,6 +75,7 @@ extern "C" int updes_solve_many(const updes_problem* problems, int32_t count, co
   }
   std::atomic<int32_t> next{0};
   std::atomic<int> first_error{UPDES_OK};
+  std::string first_text;  // written once, by the thread whose failure is reported
   auto solve_one = [&](int t, int32_t k) {
     const int32_t i = order[k];
     updes_solve_info local;
@@ -79,7 +84,8 @@ extern "C" int updes_solve_many(const updes_problem* problems, int32_t count, co
                                base + slice * size_t(t), slice, ss[t]);
     if (st) {
       int expected = UPDES_OK;
-      first_error.compare_exchange_strong(expected, st);
+      if (first_error.compare_exchange_strong(expected, st))
+        first_text = "system " + std::to_string(i) + (st == UPDES_ERR_CUDA ? ": " + updes_last_error_text() : "");
     }
   };
   // The first (largest) system on the calling thread: it also performs the library's one-time kernel
@@ -101,5 +107,7 @@ extern "C" int updes_solve_many(const updes_problem* problems, int32_t count, co
     cudaStreamSynchronize(ss[t]);
     cudaStreamDestroy(ss[t]);
   }
-  return first_error.load();
+  const int e0 = first_error.load();
+  if (e0) updes_set_last_error_text(first_text);
+  return e0;
 }

@@ -344,10 +344,21 @@ struct Carve {
 }  // namespace
 
 void updes_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  (void)cudaGetLastError();  // the failure is reported here; later checks on this thread start clean
   std::lock_guard<std::mutex> lk(g_err_mu);
   char buf[512];
   snprintf(buf, sizeof buf, "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
   g_last_error = buf;
+}
+
+void updes_set_last_error_text(const std::string& text) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error = text;
+}
+
+std::string updes_last_error_text() {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_last_error;
 }
 
 extern "C" const char* updes_last_error(void) {
@@ -433,8 +444,8 @@ __global__ void split_df_kernel(const double* __restrict__ K, int64_t ldk, float
 
 int perm_core(int n, int32_t* piv, cudaStream_t s) {
   if (n > kMaxPermN) return UPDES_ERR_UNSUPPORTED;
-  UPDES_CUDA_TRY(cudaFuncSetAttribute(perm_from_piv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(n * sizeof(int32_t))));
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)perm_from_piv_kernel, int(kMaxPermN * sizeof(int32_t)), attr)) return e;
   perm_from_piv_kernel<<<1, 1024, n * sizeof(int32_t), s>>>(piv, n, piv + n);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
