@@ -9,7 +9,9 @@ int ozaki_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t ld
                  int m, int nc, int K, DeviceStatus* st, cudaStream_t s);
 
 // The persistent, warp-specialised version (gemm_tc3.cu): digits written once per update into `scratch`
-// (ozaki3_scratch_bytes(m, nc, K) bytes, 256-byte aligned), 8 digit products, TMA-fed.
+// (ozaki3_scratch_bytes(m, nc, K) bytes, 256-byte aligned), 8 digit products, TMA-fed.  The kernel keeps one
+// CTA per SM; `max_ctas` > 0 caps its grid so that work on another stream keeps the remaining SMs.
 size_t ozaki3_scratch_bytes(int mmax, int ncmax, int Kmax);
 int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
-                  int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s);
+                  int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s,
+                  int max_ctas = 0);

@@ -603,7 +603,8 @@ size_t ozaki3_scratch_bytes(int mmax, int ncmax, int Kmax) {
 }
 
 int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
-                  int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s) {
+                  int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s,
+                  int max_ctas) {
   if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
   // the tile accumulator's low word is left unnormalised across k blocks: a few blocks only
   if (K > 1024) return UPDES_ERR_UNSUPPORTED;
@@ -641,7 +642,7 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
     UPDES_LAUNCH_CHECK();
   }
   const int ntiles = int(ceil_div(m, TM) * ceil_div(nc, TN));
-  const int grid = std::min(ntiles, num_sms_cached());
+  const int grid = std::min(ntiles, max_ctas > 0 ? std::min(max_ctas, num_sms_cached()) : num_sms_cached());
   ozaki3_kernel<<<grid, kThreads, kSmemBytes, s>>>(mapA, mapB, mapCh, mapCl, As, Bs, m, nc, Kp, st);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;

@@ -758,13 +758,81 @@ int launch_panel(void* W, const float* Wlo, int64_t ldw, TF* F, int64_t ldf, int
   return UPDES_OK;
 }
 
-constexpr int kOuterNb = 4 * kLuNb;  // 256: width of the big exact trailing updates
+constexpr int kOuterNb = 4 * kLuNb;   // 256: width of the big exact trailing updates
+constexpr int kSwapMapInts = 512;     // one panel's swap map (257 ints used): 2 KB per slot
+constexpr int kLookaheadMinN = 1024;  // smaller factorisations run their steps in order on one stream
+constexpr int kLookaheadCtas = kMaxPanelCtas;  // SMs kept for the look-ahead block beside the trailing update
 
 size_t lu_df_workspace_bytes(int n) {
-  // panel scratch (rounded up to 256 B), 2 KB swap map, digit scratch of the tensor-core update
-  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + 2048 + ozaki3_scratch_bytes(n, n, kOuterNb);
+  // panel scratch (rounded up to 256 B), the swap maps of one 256-column block's panels, the digit scratch of
+  // the trailing update and that of the look-ahead block's own updates (the two run at the same time)
+  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + size_t(kOuterNb / kLuNb) * kSwapMapInts * 4 +
+         ozaki3_scratch_bytes(n, n, kOuterNb) + ozaki3_scratch_bytes(n, kOuterNb, kLuNb);
 }
 
+namespace {
+
+// The second stream of the look-ahead and the two events that fork it from and join it back to the caller's
+// stream.  The destructor joins as well, so that every return path leaves the caller's stream ordered after
+// all work of the factorisation.
+struct SideStream {
+  cudaStream_t main = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int create(cudaStream_t s) {
+    main = s;
+    int least = 0, greatest = 0;
+    UPDES_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    UPDES_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, greatest));
+    UPDES_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    UPDES_CUDA_TRY(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    return UPDES_OK;
+  }
+  int start() {  // the side stream waits for all work issued on the caller's stream so far
+    UPDES_CUDA_TRY(cudaEventRecord(fork, main));
+    UPDES_CUDA_TRY(cudaStreamWaitEvent(side, fork, 0));
+    return UPDES_OK;
+  }
+  int finish() {  // the caller's stream waits for all work issued on the side stream so far
+    UPDES_CUDA_TRY(cudaEventRecord(join, side));
+    UPDES_CUDA_TRY(cudaStreamWaitEvent(main, join, 0));
+    return UPDES_OK;
+  }
+  ~SideStream() {
+    bool bad = false;
+    if (side && join) {
+      bad |= cudaEventRecord(join, side) != cudaSuccess;
+      bad |= cudaStreamWaitEvent(main, join, 0) != cudaSuccess;
+    }
+    if (fork) bad |= cudaEventDestroy(fork) != cudaSuccess;
+    if (join) bad |= cudaEventDestroy(join) != cudaSuccess;
+    if (side) bad |= cudaStreamDestroy(side) != cudaSuccess;
+    if (bad) (void)cudaGetLastError();
+  }
+};
+
+void add_swap_job(SwapJobs& j, int64_t& maxc, float* plane, int64_t c0, int64_t c1) {
+  if (c1 <= c0) return;
+  j.plane[j.njobs] = plane;
+  j.c0[j.njobs] = c0;
+  j.c1[j.njobs] = c1;
+  ++j.njobs;
+  maxc = std::max(maxc, c1 - c0);
+}
+
+}  // namespace
+
+// Mixed LU of the double-float matrix (Whi, Wlo) with FP32 factors overwriting Whi.  Blocks of 256 columns:
+// each block's 64-wide panels are factored with their own updates, then the block row of U is solved and the
+// trailing matrix updated by the exact tensor-core update with K = 256.
+//
+// Look-ahead (n >= kLookaheadMinN): the trailing update after block j is split into the next block's 256
+// columns, done first, and the rest.  The next block is then factored on a second stream on kLookaheadCtas
+// SMs while the rest of the update runs on the other SMs.  The two touch disjoint data as long as the next
+// block's row interchanges stay within its own columns; the interchanges of the columns outside it (the
+// factored L to its left, the trailing columns to its right) are kept as one swap map per panel and applied
+// in panel order once the update is done, the order in which the serial algorithm applies them.  Every
+// entry therefore sees the same operations in the same order and the factors are bitwise those of the
+// serial order.
 int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* ws, size_t ws_bytes, DeviceStatus* st,
                  cudaStream_t s) {
   const int nb = kLuNb;
@@ -775,89 +843,136 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   double* cand_row = reinterpret_cast<double*>(base + 256 + 2 * 1024 * sizeof(Cand));
   double* diag_row = cand_row + 2ll * 1024 * nb;
   char* after = base + ((lu_panel_workspace_bytes(nb) + 255) & ~size_t(255));
-  int32_t* swap_map = reinterpret_cast<int32_t*>(after);
-  void* digits = after + 2048;
+  int32_t* swap_maps = reinterpret_cast<int32_t*>(after);
+  char* digits = after + size_t(kOuterNb / kLuNb) * kSwapMapInts * 4;
   const size_t digits_bytes = ozaki3_scratch_bytes(n, n, kOuterNb);
+  char* digits_la = digits + digits_bytes;
+  const size_t digits_la_bytes = ozaki3_scratch_bytes(n, kOuterNb, kLuNb);
   // the persistent TMA-fed update (gemm_tc3.cu); UPDES_OZAKI=2 selects the per-tile kernel of gemm_tc.cu, which
   // also serves updates whose C planes are not 16-byte aligned
   static const bool use_v2 = [] {
     const char* v = std::getenv("UPDES_OZAKI");
     return v && v[0] == '2';
   }();
+  // UPDES_LOOKAHEAD=0 runs the block steps in order on the caller's stream (same factors, no overlap)
+  static const bool lookahead_on = [] {
+    const char* v = std::getenv("UPDES_LOOKAHEAD");
+    return !(v && v[0] == '0');
+  }();
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  UPDES_CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+  const bool lookahead = lookahead_on && !use_v2 && n >= kLookaheadMinN && cs == cudaStreamCaptureStatusNone;
   UPDES_CUDA_TRY(cudaMemsetAsync(bar, 0, 256 + 2 * 1024 * sizeof(Cand), s));  // barrier words and candidate tags
   // the single-exchange panel's records live in the candidate-row area (tags must start at zero)
   PanelRec* recs = reinterpret_cast<PanelRec*>(cand_row);
   static_assert(2 * (kMaxPanelCtas + 1) * sizeof(PanelRec) <= 2 * 1024 * kLuNb * sizeof(double), "panel records");
   UPDES_CUDA_TRY(cudaMemsetAsync(recs, 0, 2 * (kMaxPanelCtas + 1) * sizeof(PanelRec), s));
   constexpr int kOuter = kOuterNb;
-  auto swaps = [&](int k, int w) -> int {
-    SwapJobs j{};
-    int nj = 0;
-    int64_t maxc = 0;
-    if (k + w < n) {
-      j.plane[nj] = Whi; j.c0[nj] = k + w; j.c1[nj] = n; ++nj;
-      j.plane[nj] = Wlo; j.c0[nj] = k + w; j.c1[nj] = n; ++nj;
-      maxc = n - k - w;
-    }
-    if (k > 0) {
-      j.plane[nj] = Whi; j.c0[nj] = 0; j.c1[nj] = k; ++nj;
-      maxc = std::max<int64_t>(maxc, k);
-    }
-    j.njobs = nj;
-    if (!nj) return UPDES_OK;
-    StatScope sc(kStatOther, s, 0.0, 2.0 * 2 * w * maxc * 4.0 * nj);
-    swap_rows_kernel<<<dim3(unsigned(ceil_div(maxc, 64)), nj), 256, 0, s>>>(j, ld, swap_map);
+
+  auto swap_launch = [&](const SwapJobs& j, int64_t maxc, const int32_t* map, cudaStream_t us) -> int {
+    if (!j.njobs) return UPDES_OK;
+    StatScope sc(kStatOther, us, 0.0, 2.0 * 2 * nb * maxc * 4.0 * j.njobs);
+    swap_rows_kernel<<<dim3(unsigned(ceil_div(maxc, 64)), j.njobs), 256, 0, us>>>(j, ld, map);
     UPDES_LAUNCH_CHECK();
     return UPDES_OK;
   };
-  auto trsm = [&](int k, int w, int64_t c0, int64_t c1) -> int {
+  auto trsm = [&](int k, int w, int64_t c0, int64_t c1, cudaStream_t us) -> int {
     if (c1 <= c0) return UPDES_OK;
-    StatScope sc(kStatTrsm, s, double(w) * w * (c1 - c0), double(w) * (c1 - c0) * 12.0);
+    StatScope sc(kStatTrsm, us, double(w) * w * (c1 - c0), double(w) * (c1 - c0) * 12.0);
     if (w == 64) {
       static std::atomic<unsigned long long> attr{0};
       if (int e = smem_opt_in((const void*)trsm_df64_kernel, int(sizeof(TrsmDfSmem)), attr)) return e;
-      trsm_df64_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 256, sizeof(TrsmDfSmem), s>>>(Whi, Wlo, ld, k, c0, c1);
+      trsm_df64_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 256, sizeof(TrsmDfSmem), us>>>(Whi, Wlo, ld, k, c0, c1);
     } else {
-      trsm_df_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 64, 0, s>>>(Whi, Wlo, ld, k, w, c0, c1);
+      trsm_df_kernel<<<unsigned(ceil_div(c1 - c0, 64)), 64, 0, us>>>(Whi, Wlo, ld, k, w, c0, c1);
     }
     UPDES_LAUNCH_CHECK();
     return UPDES_OK;
   };
-  auto upd = [&](int r0, int r1, int c0, int c1, int kk0, int kk1) -> int {
-    // W[r0:r1, c0:c1] -= F[r0:r1, kk0:kk1] * F[kk0:kk1, c0:c1]
+  // W[r0:r1, c0:c1] -= F[r0:r1, kk0:kk1] * F[kk0:kk1, c0:c1] on stream us with digit scratch dg, at most ctas CTAs
+  auto upd = [&](int r0, int r1, int c0, int c1, int kk0, int kk1, cudaStream_t us, void* dg, size_t dgb,
+                 int ctas) -> int {
     if (!use_v2) {
       const int e3 = ozaki3_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld,
                                    Whi + int64_t(r0) * ld + kk0, ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0,
-                                   c1 - c0, kk1 - kk0, digits, digits_bytes, st, s);
+                                   c1 - c0, kk1 - kk0, dg, dgb, st, us, ctas);
       if (e3 != UPDES_ERR_UNSUPPORTED) return e3;
     }
     return ozaki_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld, Whi + int64_t(r0) * ld + kk0,
-                        ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0, c1 - c0, kk1 - kk0, st, s);
+                        ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0, c1 - c0, kk1 - kk0, st, us);
   };
-  int e;
-  for (int K0 = 0; K0 < n; K0 += kOuter) {
-    const int KE = std::min(K0 + kOuter, n);
-    for (int k = K0; k < KE; k += nb) {
+  // Columns [K0, KE): panels, their interchanges and the block's own updates.  `deferred`: the interchanges
+  // touch only the block's columns, and panel p's swap map stays in slot p for the columns outside.
+  auto factor_block = [&](int K0, int KE, bool deferred, cudaStream_t us, int ctas) -> int {
+    int e;
+    for (int k = K0, p = 0; k < KE; k += nb, ++p) {
       const int w = std::min(nb, KE - k);
-      e = launch_panel_f32(Whi, ld, n, k, w, piv, recs, swap_map, st, s);
+      int32_t* map = swap_maps + p * kSwapMapInts;
+      e = launch_panel_f32(Whi, ld, n, k, w, piv, recs, map, st, us);
       if (e == UPDES_ERR_UNSUPPORTED)
-        e = launch_panel<float, true>(Whi, Wlo, ld, Whi, ld, n, k, w, piv, bar, cand, cand_row, diag_row, swap_map,
-                                      st, s);
+        e = launch_panel<float, true>(Whi, Wlo, ld, Whi, ld, n, k, w, piv, bar, cand, cand_row, diag_row, map, st,
+                                      us);
       if (e) return e;
-      if ((e = swaps(k, w))) return e;
+      SwapJobs j{};
+      int64_t maxc = 0;
+      add_swap_job(j, maxc, Whi, k + w, deferred ? KE : n);
+      add_swap_job(j, maxc, Wlo, k + w, deferred ? KE : n);
+      add_swap_job(j, maxc, Whi, deferred ? K0 : 0, k);  // factored columns: the FP32 factors only
+      if ((e = swap_launch(j, maxc, map, us))) return e;
       if (k + w < KE) {
-        if ((e = trsm(k, w, k + w, KE))) return e;
-        if ((e = upd(k + w, n, k + w, KE, k, k + w))) return e;
+        if ((e = trsm(k, w, k + w, KE, us))) return e;
+        if ((e = upd(k + w, n, k + w, KE, k, k + w, us, deferred ? digits_la : digits,
+                     deferred ? digits_la_bytes : digits_bytes, ctas)))
+          return e;
       }
     }
-    if (KE < n) {
-      for (int b = K0; b < KE; b += nb) {
-        const int w = std::min(nb, KE - b);
-        if ((e = trsm(b, w, KE, n))) return e;
-        if (b + w < KE && (e = upd(b + w, KE, KE, n, b, b + w))) return e;
-      }
-      if ((e = upd(KE, n, KE, n, K0, KE))) return e;
+    return UPDES_OK;
+  };
+  // The deferred interchanges of block [K0, KE) on the columns outside it, panel by panel.
+  auto swaps_outside = [&](int K0, int KE) -> int {
+    for (int k = K0, p = 0; k < KE; k += nb, ++p) {
+      SwapJobs j{};
+      int64_t maxc = 0;
+      add_swap_job(j, maxc, Whi, 0, K0);
+      add_swap_job(j, maxc, Whi, KE, n);
+      add_swap_job(j, maxc, Wlo, KE, n);
+      if (int e = swap_launch(j, maxc, swap_maps + p * kSwapMapInts, s)) return e;
     }
+    return UPDES_OK;
+  };
+  // Block row of U for block [K0, KE) on the trailing columns [KE, n).
+  auto block_row = [&](int K0, int KE) -> int {
+    for (int b = K0; b < KE; b += nb) {
+      const int w = std::min(nb, KE - b);
+      if (int e = trsm(b, w, KE, n, s)) return e;
+      if (b + w < KE)
+        if (int e = upd(b + w, KE, KE, n, b, b + w, s, digits, digits_bytes, 0)) return e;
+    }
+    return UPDES_OK;
+  };
+
+  SideStream side;
+  int e;
+  if (lookahead && (e = side.create(s))) return e;
+  int K0 = 0, KE = std::min(kOuter, n);
+  if ((e = factor_block(K0, KE, false, s, 0))) return e;
+  while (KE < n) {
+    const int KE2 = std::min(KE + kOuter, n);
+    if ((e = block_row(K0, KE))) return e;
+    if ((e = upd(KE, n, KE, KE2, K0, KE, s, digits, digits_bytes, 0))) return e;  // the next block's columns
+    if (lookahead && KE2 < n) {
+      if ((e = side.start())) return e;
+      if ((e = factor_block(KE, KE2, true, side.side, kLookaheadCtas))) return e;
+      const int rest_ctas = std::max(num_sms() - kLookaheadCtas, num_sms() / 2);
+      if ((e = upd(KE, n, KE2, n, K0, KE, s, digits, digits_bytes, rest_ctas))) return e;
+      if ((e = side.finish())) return e;
+      if ((e = swaps_outside(KE, KE2))) return e;
+    } else {
+      if (KE2 < n && (e = upd(KE, n, KE2, n, K0, KE, s, digits, digits_bytes, 0))) return e;
+      if ((e = factor_block(KE, KE2, false, s, 0))) return e;
+    }
+    K0 = KE;
+    KE = KE2;
   }
   return UPDES_OK;
 }
