@@ -115,6 +115,23 @@ UPDES_API int updes_assemble(const updes_problem* p, double* K64, int64_t ld64, 
                    void* stream);
 
 /*
+ * The same K for a polyharmonic kernel (UPDES_ERR_UNSUPPORTED otherwise), evaluated in
+ * double-float arithmetic on the FP32 pipes and written unscaled as two FP32
+ * planes: Khi = FP32 rounding of the entry, Klo = FP32 rounding of the rest
+ * (hi + lo within a few units of 2^-48 of the entry).  Columns n..ld-1 are
+ * written as zero; ld a multiple of 4, planes 16-byte aligned.  rowmax (device,
+ * n, may be NULL, must start at zero) receives each row's max |hi| as float
+ * bits; range_flag (device, may be NULL) is set to 1 if an entry is not finite
+ * or nonzero below 2^-100 in magnitude (then use updes_assemble).  scratch:
+ * device, updes_assemble_df_scratch() bytes, 16-byte aligned.  The mixed-precision
+ * solve assembles polyharmonic systems this way.  Same matrix as assemble_A's
+ * blocks (updes/assembly.py:62-362), different arithmetic.
+ */
+UPDES_API int updes_assemble_df_scratch(const updes_problem* p, size_t* bytes);
+UPDES_API int updes_assemble_df(const updes_problem* p, float* Khi, float* Klo, int64_t ld, uint32_t* rowmax,
+                   int32_t* range_flag, void* scratch, size_t scratch_bytes, void* stream);
+
+/*
  * vals = [Phi P] c at the nodes (Phi_ii = 0 unless self_term), FP64,
  * regenerating Phi on the fly.  coeffs: device, n; vals: device, N.
  * Replaces the `vals` of the reference, which come out of its QR solve

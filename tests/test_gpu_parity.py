@@ -116,6 +116,66 @@ def test_mat_materialises_reference_B():
     assert rel(B, g["B"]) < 1e-9
 
 
+# Double-float assembly: every polyharmonic golden case, plus polyharmonic variants of the periodic and the
+# Robin (Gaussian) cases so that every row kind is covered (r^3 and r^5).
+DF_CASES = [nm for nm in NAMES if C.CASES[nm]["rbf"][0] == "polyharmonic"] + [
+    "periodic_imq_8x7@1", "gaussian_dnr_9x8@2", "thinplate_deg4_8x8@1"]
+
+
+def _df_case(name):
+    base, _, a = name.partition("@")
+    case = dict(C.CASES[base])
+    if a:
+        case["rbf"] = ("polyharmonic", int(a))
+    return case
+
+
+def _assemble_df(dp):
+    import torch
+    lib = _lib.load()
+    ld = int(lib.updes_matrix_ld(dp.n, 8))
+    hi = torch.full((dp.n, ld), float("nan"), dtype=torch.float32, device="cuda")
+    lo = torch.full((dp.n, ld), float("nan"), dtype=torch.float32, device="cuda")
+    rowmax = torch.zeros(dp.n, dtype=torch.int32, device="cuda")
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nb = ctypes.c_size_t()
+    _lib.check(lib.updes_assemble_df_scratch(ctypes.byref(dp.c), ctypes.byref(nb)), "scratch")
+    scratch = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
+    st = lib.updes_assemble_df(ctypes.byref(dp.c), hi.data_ptr(), lo.data_ptr(), ld, rowmax.data_ptr(),
+                               flag.data_ptr(), scratch.data_ptr(), nb.value, dp.stream())
+    torch.cuda.synchronize()
+    return st, hi, lo, rowmax, flag, ld
+
+
+@pytest.mark.parametrize("name", DF_CASES)
+def test_df_assembly_matches_fp64(name):
+    """The double-float planes hi + lo agree with the FP64 assembly to 2^-45 of each row's largest entry
+    (the FP64 entries are themselves good to ~2^-50); padding columns are zero, the row maxima are those of
+    |hi|, and no entry is flagged out of range."""
+    case = _df_case(name)
+    cl, dp, q = device_problem(case)
+    K64, _, ld = assemble(dp)
+    st, hi, lo, rowmax, flag, ld2 = _assemble_df(dp)
+    _lib.check(st, "updes_assemble_df")
+    assert ld2 == ld and int(flag.item()) == 0
+    n = dp.n
+    K = K64.cpu().numpy()
+    H, L = hi.cpu().numpy(), lo.cpu().numpy()
+    assert np.all(H[:, n:] == 0) and np.all(L[:, n:] == 0)
+    D = H[:, :n].astype(np.float64) + L[:, :n].astype(np.float64)
+    rmax = np.abs(K[:, :n]).max(axis=1)
+    err = np.abs(D - K[:, :n]).max(axis=1)
+    assert np.all(err <= 2.0 ** -45 * rmax), (err / rmax).max()
+    assert np.all(np.abs(L[:, :n]) <= np.spacing(np.abs(H[:, :n])))  # normalised pairs
+    want = np.abs(H[:, :n]).max(axis=1).astype(np.float32).view(np.int32)
+    assert np.array_equal(rowmax.cpu().numpy(), want)
+
+
+def test_df_assembly_rejects_other_kernels():
+    cl, dp, q = device_problem(C.CASES["gaussian_dnr_9x8"])
+    st = _assemble_df(dp)[0]
+    assert st == _lib.ERR_UNSUPPORTED
+
 def _rand_system(n, seed):
     rng = np.random.default_rng(seed)
     A = rng.standard_normal((n, n)) + 0.5 * np.eye(n)

@@ -86,6 +86,9 @@ SIGNATURES = {
     "updes_last_error": (ctypes.c_char_p, []),
     "updes_matrix_ld": (_i64, [_i64, _i32]),
     "updes_assemble": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _i64, _vp, _i64, _vp]),
+    "updes_assemble_df_scratch": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.POINTER(ctypes.c_size_t)]),
+    "updes_assemble_df": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _i64, _vp, _vp, _vp, ctypes.c_size_t,
+                                         _vp]),
     "updes_eval_values": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp]),
     "updes_eval_field": (ctypes.c_int, [_i32, _vp, _i32, _vp, _i32, _i32, _f64, _vp, _i32, _vp, _vp]),
     "updes_lu_workspace": (ctypes.c_int, [_i32, _i32, ctypes.POINTER(_sz)]),

@@ -4,6 +4,7 @@
 // block of assemble_A (updes/assembly.py:93-362, 62-85); updes_eval_values
 // evaluates vals = [Phi P] c (updes/assembly.py:404-410 read backwards).
 #include "common.cuh"
+#include "df.cuh"
 #include "rbf.cuh"
 #include "stats.cuh"
 
@@ -452,6 +453,171 @@ __global__ void __launch_bounds__(256) eval_values_batch_kernel(updes_problem p,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float assembly of polyharmonic systems (the mixed-precision solve's K)
+// ---------------------------------------------------------------------------
+// GB300 runs FP64 at 1/64 of its FP32 rate, and the FP64 entries of an r^k kernel (square root, powers and
+// the operator's combination, ~30 FP64 operations each) bind assemble_kernel to the FP64 pipe.  The mixed
+// solve keeps K as two FP32 planes (48 significant bits) anyway, so here the entries are evaluated in
+// double-float arithmetic on the FP32 pipes:
+//  - node coordinates as exact triple-float expansions, so that x_i - x_j is formed exactly and rounded
+//    once to double-float;
+//  - for a row with operator weights w (value, d/dx, d/dy, d2/dx2, d2/dy2) and k = 2a+1,
+//        K_ij = r^(k-2) (A0 r^2 + A1 dx + A2 dy + A3 + (A4 dx^2 + A5 dy^2) / r^2)
+//    with A = (w0, k w1, k w2, k (w3 + w4), k (k-2) w3, k (k-2) w4) for interior rows (the closed forms
+//    phi = r^k, g1 = k r^(k-2), g2 = k (k-2) r^(k-4) of rbf_g), A = (1, 0, 0, 0, 0, 0) for Dirichlet,
+//    (0, k n1x, k n1y, 0, 0, 0) for Neumann and (beta, k n1x, k n1y, 0, 0, 0) for Robin rows; the entry is
+//    0 at r = 0 as in the FP64 kernel (phi(0) = 0, derivatives 0 there);
+//  - monomial columns, P^T rows and periodic rows (a few per system) in FP64 through entry_rbf/entry_mono.
+// The planes are written unscaled, with the row maxima of |hi|; the equilibration follows in the caller.
+
+constexpr float kDfTiny = 7.88860905e-31f;  // 2^-100: below it an entry's low word would leave the normal range
+
+struct __align__(16) DfRow {
+  int kind, a, pad0, pad1;  // row kind (-1 interior, UPDES_ROW_*), evaluation node
+  float c[12];              // A0..A5 as double-float pairs
+};
+
+__global__ void assemble_df_setup_kernel(updes_problem p, DfRow* __restrict__ rows, float* __restrict__ tri) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.N) return;
+  for (int d = 0; d < 2; ++d) {  // exact triple-float expansion of each coordinate
+    const double x = p.nodes[2ll * j + d];
+    const float x0 = __double2float_rn(x);
+    const double r1 = x - double(x0);
+    const float x1 = __double2float_rn(r1);
+    tri[6ll * j + 3 * d] = x0;
+    tri[6ll * j + 3 * d + 1] = x1;
+    tri[6ll * j + 3 * d + 2] = __double2float_rn(r1 - double(x1));
+  }
+  const RowInfo ri = load_row(p, j);
+  const double k = 2.0 * p.rbf_param + 1.0;
+  double A[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (ri.kind == -1) {
+    A[0] = ri.w0; A[1] = k * ri.w1; A[2] = k * ri.w2; A[3] = k * (ri.w3 + ri.w4);
+    A[4] = k * (k - 2.0) * ri.w3; A[5] = k * (k - 2.0) * ri.w4;
+  } else if (ri.kind == UPDES_ROW_DIRICHLET) {
+    A[0] = 1.0;
+  } else if (ri.kind == UPDES_ROW_NEUMANN || ri.kind == UPDES_ROW_ROBIN) {
+    A[0] = ri.kind == UPDES_ROW_ROBIN ? ri.beta : 0.0;
+    A[1] = k * ri.n1x; A[2] = k * ri.n1y;
+  }
+  DfRow o;
+  o.kind = ri.kind;
+  o.a = ri.a;
+  o.pad0 = o.pad1 = 0;
+  for (int t = 0; t < 6; ++t) {
+    const F2 v = df_from_double(A[t]);
+    o.c[2 * t] = v.h;
+    o.c[2 * t + 1] = v.l;
+  }
+  rows[j] = o;
+}
+
+__global__ void __launch_bounds__(256) assemble_df_kernel(updes_problem p, int n, const DfRow* __restrict__ rows,
+                                                          const float* __restrict__ tri, float* __restrict__ Khi,
+                                                          float* __restrict__ Klo, int64_t ld,
+                                                          unsigned* __restrict__ rowmax, int* __restrict__ range_flag) {
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int64_t c0 = int64_t(blockIdx.x) * kAsmCols + 4 * lane;
+  const bool live = c0 < ld;  // every lane stays for the row-maximum shuffles
+  const int apow = int(p.rbf_param);  // r^(k-2) = r * (r^2)^(a-1)
+  const int ip = 2 * apow + 1;
+  float cx[4][3], cy[4][3];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int64_t c = c0 + u;
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      cx[u][t] = c < p.N ? tri[6 * c + t] : 0.f;
+      cy[u][t] = c < p.N ? tri[6 * c + 3 + t] : 0.f;
+    }
+  }
+  bool bad = false;
+  const int rbase = blockIdx.y * kAsmRows + warp * kAsmRowsPerWarp;
+  for (int i = 0; i < kAsmRowsPerWarp; ++i) {
+    const int r = rbase + i;
+    if (r >= n) break;
+    float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+    const int kind = r < p.N ? rows[r].kind : -2;
+    if (live && kind >= -1 && kind <= UPDES_ROW_ROBIN) {
+      const DfRow& R = rows[r];
+      const F2 A0{R.c[0], R.c[1]}, A1{R.c[2], R.c[3]}, A2{R.c[4], R.c[5]};
+      const F2 A3{R.c[6], R.c[7]}, A4{R.c[8], R.c[9]}, A5{R.c[10], R.c[11]};
+      const int a = R.a;
+      const float ax0 = tri[6ll * a], ax1 = tri[6ll * a + 1], ax2 = tri[6ll * a + 2];
+      const float ay0 = tri[6ll * a + 3], ay1 = tri[6ll * a + 4], ay2 = tri[6ll * a + 5];
+      const bool interior = kind == -1;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t c = c0 + u;
+        if (c < p.N) {
+          const F2 dx = diff3(ax0, ax1, ax2, cx[u][0], cx[u][1], cx[u][2]);
+          const F2 dy = diff3(ay0, ay1, ay2, cy[u][0], cy[u][1], cy[u][2]);
+          if (dx.h == 0.f && dy.h == 0.f) continue;  // r = 0: the entry is 0
+          const F2 dx2 = df_sqr(dx), dy2 = df_sqr(dy);
+          const F2 r2 = df_add(dx2, dy2);
+          F2 rk2 = df_sqrt(r2);
+          for (int t = 1; t < apow; ++t) rk2 = df_mul(rk2, r2);
+          F2 br{0.f, 0.f};
+          if (A0.h != 0.f) br = df_mul(A0, r2);
+          if (A1.h != 0.f) br = df_add(br, df_mul(A1, dx));
+          if (A2.h != 0.f) br = df_add(br, df_mul(A2, dy));
+          if (interior) {
+            br = df_add(br, A3);
+            if (A4.h != 0.f || A5.h != 0.f) br = df_add(br, df_div(df_add(df_mul(A4, dx2), df_mul(A5, dy2)), r2));
+          }
+          const F2 v = df_mul(rk2, br);
+          hi[u] = v.h;
+          lo[u] = v.l;
+        } else if (c < n) {
+          const RowInfo ri = load_row(p, r);
+          const F2 v = df_from_double(entry_mono(ri, int(c - p.N)));
+          hi[u] = v.h;
+          lo[u] = v.l;
+        }
+      }
+    } else if (live) {  // P^T and periodic rows in FP64
+      const RowInfo ri = load_row(p, r);
+      const double param = p.rbf_param;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t c = c0 + u;
+        double v = 0.0;
+        if (c < p.N) v = entry_rbf<UPDES_RBF_POLYHARMONIC>(ri, int(c), p.nodes[2 * c], p.nodes[2 * c + 1], param, ip,
+                                                           p.self_term);
+        else if (c < n) v = entry_mono(ri, int(c - p.N));
+        const F2 f = df_from_double(v);
+        hi[u] = f.h;
+        lo[u] = f.l;
+      }
+    }
+    float m = 0.f;
+    if (live) {
+      float* dh = Khi + int64_t(r) * ld + c0;
+      float* dl = Klo + int64_t(r) * ld + c0;
+      if (c0 + 3 < ld) {
+        *reinterpret_cast<float4*>(dh) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<float4*>(dl) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+      } else {
+        for (int u = 0; u < 4 && c0 + u < ld; ++u) {
+          dh[u] = hi[u];
+          dl[u] = lo[u];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float ah = fabsf(hi[u]);
+        m = fmaxf(m, ah);
+        bad |= !(ah <= 3.0e38f) || (ah != 0.f && ah < kDfTiny);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m > 0.f && rowmax) atomicMax(rowmax + r, __float_as_uint(m));
+  }
+  if (bad && range_flag) atomicExch(range_flag, 1);
+}
+
 int check_problem(const updes_problem* p) {
   if (!p || p->N <= 0 || p->Ni < 0 || p->Ni > p->N) return UPDES_ERR_INVALID;
   if (!(p->M == 1 || p->M == 3 || p->M == 6 || p->M == 10 || p->M == 15)) return UPDES_ERR_INVALID;
@@ -495,6 +661,39 @@ extern "C" int updes_assemble(const updes_problem* p, double* K64, int64_t ld64,
     default:
       assemble_kernel<UPDES_RBF_THIN_PLATE><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
   }
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+extern "C" int updes_assemble_df_scratch(const updes_problem* p, size_t* bytes) {
+  if (check_problem(p) || !bytes) return UPDES_ERR_INVALID;
+  *bytes = ((size_t(p->N) * sizeof(DfRow) + 255) & ~size_t(255)) + size_t(p->N) * 6 * sizeof(float) + 256;
+  return UPDES_OK;
+}
+
+extern "C" int updes_assemble_df(const updes_problem* p, float* Khi, float* Klo, int64_t ld, uint32_t* rowmax,
+                                 int32_t* range_flag, void* scratch, size_t scratch_bytes, void* stream) {
+  int st = check_problem(p);
+  if (st) return st;
+  if (p->rbf != UPDES_RBF_POLYHARMONIC) return UPDES_ERR_UNSUPPORTED;
+  const int n = p->N + p->M;
+  if (!Khi || !Klo || ld < n || ld % 4 || !scratch) return UPDES_ERR_INVALID;
+  if (((reinterpret_cast<uintptr_t>(Khi) | reinterpret_cast<uintptr_t>(Klo) | reinterpret_cast<uintptr_t>(scratch)) &
+       15) != 0)
+    return UPDES_ERR_INVALID;
+  size_t need = 0;
+  updes_assemble_df_scratch(p, &need);
+  if (scratch_bytes < need) return UPDES_ERR_WORKSPACE;
+  DfRow* rows = static_cast<DfRow*>(scratch);
+  float* tri = reinterpret_cast<float*>(static_cast<char*>(scratch) +
+                                        ((size_t(p->N) * sizeof(DfRow) + 255) & ~size_t(255)));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  StatScope sc(kStatAssemble, s, 0.0, double(n) * ld * 8.0);
+  assemble_df_setup_kernel<<<unsigned(ceil_div(p->N, 256)), 256, 0, s>>>(*p, rows, tri);
+  UPDES_LAUNCH_CHECK();
+  dim3 block(32, kAsmWarps);
+  dim3 grid(unsigned(ceil_div(ld, kAsmCols)), unsigned(ceil_div(n, kAsmRows)));
+  assemble_df_kernel<<<grid, block, 0, s>>>(*p, n, rows, tri, Khi, Klo, ld, rowmax, range_flag);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }

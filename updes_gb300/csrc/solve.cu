@@ -3,6 +3,7 @@
 // updes_solve replaces pde_solver's assemble_B -> lineax QR ->
 // core_compute_coefficients sequence (updes/operators.py:602-618) by one
 // factorisation of the augmented Kansa matrix K and refinement in FP64.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -91,6 +92,49 @@ __global__ void col_scale_kernel(int n, double* __restrict__ dc) {
   dc[j] = ldexp(1.0, -e);
 }
 
+
+// dr[i] = 2^-e with the row maximum (FP32 bit pattern in maxbits) in [2^(e-1), 2^e)
+__global__ void row_scale_bits_kernel(const unsigned* __restrict__ maxbits, int n, double* __restrict__ dr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double m = double(__uint_as_float(maxbits[i]));
+  int e = 0;
+  if (m > 0.0 && isfinite(m)) frexp(m, &e);
+  dr[i] = ldexp(1.0, -e);
+}
+
+// Column maxima of |Khi| diag(dr) (the FP32 plane of an unscaled double-float K), as col_max_kernel.
+__global__ void col_max_f32_kernel(const float* __restrict__ Khi, int64_t ld, int n, const double* __restrict__ dr,
+                                   unsigned long long* __restrict__ colmax) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int rows = int(ceil_div(n, kColScaleChunks));
+  const int i0 = blockIdx.y * rows, i1 = min(n, i0 + rows);
+  double m = 0.0;
+  for (int i = i0; i < i1; ++i) m = fmax(m, double(fabsf(Khi[int64_t(i) * ld + j])) * dr[i]);
+  if (m > 0.0) atomicMax(colmax + j, (unsigned long long)__double_as_longlong(m));
+}
+
+// Both planes times dr_i dc_j in place (powers of two: exact), four columns a thread, rows strided over grid.y.
+__global__ void __launch_bounds__(256) scale_planes_kernel(float* __restrict__ hi, float* __restrict__ lo, int64_t ld,
+                                                           int n, const double* __restrict__ dr,
+                                                           const double* __restrict__ dc) {
+  const int64_t j0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
+  if (j0 >= n) return;
+  float cs[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) cs[u] = j0 + u < n ? float(dc[j0 + u]) : 1.f;
+  for (int i = blockIdx.y; i < n; i += gridDim.y) {
+    const float rs = float(dr[i]);
+    float4* ph = reinterpret_cast<float4*>(hi + int64_t(i) * ld + j0);
+    float4* pl = reinterpret_cast<float4*>(lo + int64_t(i) * ld + j0);
+    float4 h = *ph, l = *pl;
+    h.x = h.x * rs * cs[0]; h.y = h.y * rs * cs[1]; h.z = h.z * rs * cs[2]; h.w = h.w * rs * cs[3];
+    l.x = l.x * rs * cs[0]; l.y = l.y * rs * cs[1]; l.z = l.z * rs * cs[2]; l.w = l.w * rs * cs[3];
+    *ph = h;
+    *pl = l;
+  }
+}
 
 // out_i = dr_i * (bsign * b_i + ksign * sum_j K_ij dc_j x_j), one warp per row (dr, dc, b may be null)
 // With absout != null also writes absout_i = dr_i * (sum_j |K_ij dc_j x_j| + |b_i|) (backward-error denominators).
@@ -267,6 +311,10 @@ constexpr int kDotBlocks = 120;
 // from the double-float planes of K (48 significant bits per entry), which by themselves put the
 // measured backward error of an FP64 LU solution at roughly 50-100 unit roundoffs.
 constexpr double kBwdFloor = 256.0 * 1.1102230246251565e-16;
+// A restart cycle stops its inner iteration once the estimated residual has fallen by this factor: the
+// update it then applies goes through the FP32 factors, whose solves are accurate to about 1e-6 of the
+// correction, so the true residual cannot follow the estimate further within one cycle.
+constexpr double kInnerReduction = 1e-6;
 
 // partial[b * nv + i] = sum over block b's chunk of V_i . w
 __global__ void __launch_bounds__(256) multi_dot_kernel(const double* __restrict__ V, int64_t ldv, int nv,
@@ -789,6 +837,10 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
       stalls = 0;
     }
     last_beta = beta;
+    // this cycle stops at whichever comes first: the requested tolerance, the reduction one cycle can
+    // deliver, or (with a factor 2 to spare) the reduction that brings the backward error to its floor (the
+    // ratio backward error / residual norm changes little between cycles)
+    const double target = std::max(o.tol * bnorm, beta * std::max(kInnerReduction, 0.5 * kBwdFloor / bwd));
     // V0 = r / beta
     axpby_kernel<<<g, 256, 0, s>>>(w.V, 1.0 / beta, w.r, 0.0, n, nullptr);
     UPDES_LAUNCH_CHECK();
@@ -833,7 +885,7 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
       for (int i = 0; i <= j; ++i) H[size_t(i) * m + j] = hcol[i];
       if (trace_on())
         std::fprintf(stderr, "[updes gmres]   j=%d estimate=%.3e h_next=%.3e\n", j, std::fabs(gv[j + 1]) / bnorm, hn);
-      if (std::fabs(gv[j + 1]) <= o.tol * bnorm || hn == 0.0) {
+      if (std::fabs(gv[j + 1]) <= target || hn == 0.0) {
         ++j;
         ++total;
         break;
@@ -913,10 +965,57 @@ int read_state(const SolveWs& w, int n, int* precision, cudaStream_t s) {
   return UPDES_OK;
 }
 
-// Assemble K (FP64) and its power-of-two equilibration.
-int assemble_stage(const updes_problem* p, const SolveWs& w, int n, updes_solve_info* info, cudaStream_t s) {
+// K of a polyharmonic system in double-float (updes_assemble_df) with the power-of-two equilibration of the
+// FP64 path: row maxima from the assembly, column maxima of the row-scaled hi plane, both planes scaled in
+// place.  UNSUPPORTED when an entry falls outside the range in which double-float keeps its 48 bits (the
+// caller then assembles in FP64).
+int assemble_df_stage(const updes_problem* p, const SolveWs& w, int n, cudaStream_t s) {
+  unsigned* rowmax = reinterpret_cast<unsigned*>(w.dc);  // float bits, then the column maxima, then dc
+  int32_t* flag = reinterpret_cast<int32_t*>(w.r);       // free until the refinement
+  UPDES_CUDA_TRY(cudaMemsetAsync(rowmax, 0, size_t(n) * sizeof(unsigned), s));
+  UPDES_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int32_t), s));
+  // the FP64 working matrix is free until the factorisation: the assembly's row records and coordinates
+  int e = updes_assemble_df(p, w.Khi, w.Klo, w.ld, rowmax, flag, w.W, size_t(n) * w.ld * sizeof(double), s);
+  if (e) return e;
+  row_scale_bits_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(rowmax, n, w.dr);
+  UPDES_LAUNCH_CHECK();
+  UPDES_CUDA_TRY(cudaMemsetAsync(w.dc, 0, size_t(n) * sizeof(double), s));
+  col_max_f32_kernel<<<dim3(unsigned(ceil_div(n, 256)), kColScaleChunks), 256, 0, s>>>(
+      w.Khi, w.ld, n, w.dr, reinterpret_cast<unsigned long long*>(w.dc));
+  UPDES_LAUNCH_CHECK();
+  col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(n, w.dc);
+  UPDES_LAUNCH_CHECK();
+  {
+    StatScope sc(kStatOther, s, 0.0, double(n) * n * 16.0);
+    scale_planes_kernel<<<dim3(unsigned(ceil_div(n, 1024)), unsigned(std::min(n, 4096))), 256, 0, s>>>(
+        w.Khi, w.Klo, w.ld, n, w.dr, w.dc);
+    UPDES_LAUNCH_CHECK();
+  }
+  int32_t hflag = 0;
+  UPDES_CUDA_TRY(cudaMemcpyAsync(&hflag, flag, sizeof hflag, cudaMemcpyDeviceToHost, s));
+  UPDES_CUDA_TRY(cudaStreamSynchronize(s));
+  return hflag ? UPDES_ERR_UNSUPPORTED : UPDES_OK;
+}
+
+// Assemble K and its power-of-two equilibration into the double-float planes: in double-float arithmetic for
+// a polyharmonic system factored in FP32, else in FP64.
+int assemble_stage(const updes_problem* p, const SolveWs& w, int n, int precision, updes_solve_info* info,
+                   cudaStream_t s) {
   Timer t(s);
   int e;
+  // UPDES_DF_ASSEMBLY=0 assembles every system in FP64
+  static const bool df_assembly = [] {
+    const char* v = std::getenv("UPDES_DF_ASSEMBLY");
+    return !(v && v[0] == '0');
+  }();
+  if (df_assembly && precision == UPDES_PREC_FP32 && p->rbf == UPDES_RBF_POLYHARMONIC) {
+    e = assemble_df_stage(p, w, n, s);
+    if (e != UPDES_ERR_UNSUPPORTED) {
+      if (e) return e;
+      info->t_assemble_ms += t.stop();
+      return UPDES_OK;
+    }
+  }
   if ((e = updes_assemble(p, w.W, w.ld, nullptr, 0, s))) return e;  // FP64 K, staged in the working buffer
   row_scale_kernel<<<unsigned(ceil_div(int64_t(n) * 32, 256)), 256, 0, s>>>(w.W, w.ld, n, w.dr);
   UPDES_LAUNCH_CHECK();
@@ -1014,7 +1113,7 @@ extern "C" int updes_factor(const updes_problem* p, const updes_solve_opts* opts
   std::memset(info, 0, sizeof *info);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n = p->N + p->M;
-  if ((e = assemble_stage(p, w, n, info, s))) return e;
+  if ((e = assemble_stage(p, w, n, o.precision, info, s))) return e;
   if ((e = factor_stage(w, n, o.precision, info, s))) return e;
   return info->lu_info ? UPDES_ERR_SINGULAR : UPDES_OK;
 }
@@ -1066,7 +1165,7 @@ extern "C" int updes_solve(const updes_problem* p, const double* q, double* coef
   std::memset(info, 0, sizeof *info);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n = p->N + p->M;
-  if ((e = assemble_stage(p, w, n, info, s))) return e;
+  if ((e = assemble_stage(p, w, n, o.precision, info, s))) return e;
   if ((e = factor_stage(w, n, o.precision, info, s))) return e;
   if ((e = solve_stage(p, w, n, q, 1, coeffs, 1, vals, 1, o, info, s))) return e;
   if (info->lu_info) return UPDES_ERR_SINGULAR;
