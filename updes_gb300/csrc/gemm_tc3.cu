@@ -75,15 +75,19 @@ __device__ __forceinline__ int exp_of(float mx) {
   return max(E - 126, -100);
 }
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+// Error-free sum (Knuth's TwoSum) and Dekker's Fast2Sum on column pairs, with the packed FP32x2 instructions
+// of sm_100+ (one issue slot per pair).  y - x is formed as fma(x, -1, y): the product is exact, so it rounds once like a subtraction.
+__device__ __forceinline__ float2 sub2(float2 y, float2 x) { return __ffma2_rn(x, make_float2(-1.f, -1.f), y); }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = sub2(s, a);
+  e = __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb));
 }
 
-__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  e = __fsub_rn(b, __fsub_rn(s, a));
+__device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  e = sub2(b, sub2(s, a));
 }
 
 // ---- mbarrier / tcgen05 / TMA primitives -------------------------------------------------------------
@@ -154,14 +158,14 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(taddr)
                : "memory");
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -225,13 +229,13 @@ __global__ void digits_rows_kernel(const float* __restrict__ A, int64_t lda, int
   }
 }
 
-// B (K x nc, ldb) -> Bd[p][c][k] (bf16, transposed) and Bs[c][kb]; a CTA per (64 k, 64 columns) tile.
+// B (K x nc, ldb) -> Bd[p][c][k] (bf16, transposed) and Bs[kb][c] (row stride ncp = nc rounded up to TN, the
+// padding columns 0); a CTA per (64 k, 64 columns) tile.
 __global__ void __launch_bounds__(256) digits_cols_kernel(const float* __restrict__ B, int64_t ldb, int nc, int K,
                                                           int Kp, __nv_bfloat16* __restrict__ Bd,
                                                           float* __restrict__ Bs) {
   __shared__ float t[TK][TN + 1];
   const int kb = blockIdx.y, c0 = blockIdx.x * TN;
-  const int nkb = Kp / TK;
   for (int e = threadIdx.x; e < TK * TN; e += blockDim.x) {
     const int k = e / TN, c = e % TN;
     const int gk = kb * TK + k, gc = c0 + c;
@@ -239,15 +243,19 @@ __global__ void __launch_bounds__(256) digits_cols_kernel(const float* __restric
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ncp = ceil_div(nc, TN) * TN;
   for (int c = warp; c < TN; c += blockDim.x / 32) {
     const int gc = c0 + c;
-    if (gc >= nc) continue;
+    if (gc >= nc) {
+      if (lane == 0) Bs[kb * ncp + gc] = 0.f;
+      continue;
+    }
     float v[2] = {t[lane][c], t[lane + 32][c]};
     float mx = fmaxf(fabsf(v[0]), fabsf(v[1]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     const int e = exp_of(mx);
-    if (lane == 0) Bs[int64_t(gc) * nkb + kb] = pow2f(e - 8);
+    if (lane == 0) Bs[kb * ncp + gc] = pow2f(e - 8);
     const float scale = pow2f(8 - e);
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -270,6 +278,7 @@ struct Ctrl {
   int abort_flag;
 };
 
+// 18 warps: a sub-partition holds up to 5 of them in its 16,384 registers, so at most 96 registers a thread
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki3_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   const __grid_constant__ CUtensorMap tmCh, const __grid_constant__ CUtensorMap tmCl,
@@ -282,6 +291,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tiles_n = int(ceil_div(nc, TN)), tiles_m = int(ceil_div(m, TM));
   const int ntiles = tiles_n * tiles_m;
+  const int64_t ncp = int64_t(tiles_n) * TN;  // row stride of the column scales
   const int nkb = Kp / TK;
   volatile int* abort_flag = &ctl.abort_flag;
 
@@ -412,17 +422,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
       const int r0 = (t / tiles_n) * TM, c0 = (t % tiles_n) * TN;
       const int gr = r0 + row_in_tile;
-      float acc_h[kEpiCols], acc_l[kEpiCols];
+      // accumulators of the thread's row over its kEpiCols columns, as column pairs
+      float2 acc_h[kEpiCols / 2], acc_l[kEpiCols / 2];
 #pragma unroll
-      for (int u = 0; u < kEpiCols; ++u) { acc_h[u] = 0.f; acc_l[u] = 0.f; }
+      for (int u = 0; u < kEpiCols / 2; ++u) { acc_h[u] = make_float2(0.f, 0.f); acc_l[u] = make_float2(0.f, 0.f); }
       bool ok = true;
       for (int kb = 0; kb < nkb; ++kb, ++j) {
         const int set = j & 1;
         const uint32_t tph = uint32_t(j >> 1) & 1u;
-        // scales of this k block (loaded before the wait): the row's, and one column's per lane
+        // scales of this k block: the row's (loaded before the wait) and, per chunk of four columns, the
+        // columns' (the same 16-byte vector for every lane: one broadcast load)
         const float sa = gr < m ? __ldg(As + int64_t(gr) * nkb + kb) : 0.f;
-        const int my_c = c0 + colbase + lane;
-        const float my_sb = (lane < kEpiCols && my_c < nc) ? __ldg(Bs + int64_t(my_c) * nkb + kb) : 0.f;
+        const float4* sbp = reinterpret_cast<const float4*>(Bs + int64_t(kb) * ncp + c0 + colbase);
         // every wait ends in a warp vote, so a warp always leaves together (tcgen05.ld needs all 32 lanes)
         if (!__all_sync(0xffffffffu, mbar_wait(&ctl.tfull[set], tph, abort_flag))) {
           if (lane == 0 && !*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 43); }
@@ -432,36 +443,41 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
 #pragma unroll
-        for (int ch = 0; ch < kEpiCols / 8; ++ch) {
-          const int col = colbase + ch * 8;
-          float g[kGroups][8];
+        for (int ch = 0; ch < kEpiCols / 4; ++ch) {
+          const int col = colbase + ch * 4;
+          const float4 s4 = __ldg(sbp + ch);
+          float g[kGroups][4];
 #pragma unroll
           for (int gi = 0; gi < kGroups; ++gi)
-            tmem_ld8(tmem + lane_base + uint32_t(set * kGroups * TN + gi * TN + col), g[gi]);
+            tmem_ld4(tmem + lane_base + uint32_t(set * kGroups * TN + gi * TN + col), g[gi]);
           tmem_wait_ld();
-          if (ch == kEpiCols / 8 - 1) {
+          if (ch == kEpiCols / 4 - 1) {
             // every chunk has been read: release the accumulator set to the MMA issuer
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.tempty[set]);
           }
+          const float2 c9 = make_float2(1.953125e-3f, 1.953125e-3f);          // 2^-9
+          const float2 c18 = make_float2(3.814697265625e-06f, 3.814697265625e-06f);  // 2^-18
+          const float2 sa2 = make_float2(sa, sa);
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const float sb = __shfl_sync(0xffffffffu, my_sb, ch * 8 + u);
+          for (int u = 0; u < 4; u += 2) {
+            const int cu = ch * 4 + u;  // the pair's first column among the thread's kEpiCols
+            const float2 sb2 = u ? make_float2(s4.z, s4.w) : make_float2(s4.x, s4.y);
             // k-block value = g0 + 2^-9 g1 + 2^-18 (g2 + 2^-9 g3): g0 + 2^-9 g1 exactly as (hh, ll); the two
             // small groups merged in one rounding (about 2^-40 of the block's scale, far below the digit cut)
-            float hh, ll;
-            two_sum(g[0][u], __fmul_rn(g[1][u], 1.953125e-3f), hh, ll);
-            const float g23 = __fmaf_rn(g[3][u], 1.953125e-3f, g[2][u]);
-            ll = __fmaf_rn(g23, 3.814697265625e-06f, ll);
-            const float sc = __fmul_rn(sa, sb);  // power of two: exact
-            hh = __fmul_rn(hh, sc);
-            ll = __fmul_rn(ll, sc);
+            float2 hh, ll;
+            two_sum2(make_float2(g[0][u], g[0][u + 1]), __fmul2_rn(make_float2(g[1][u], g[1][u + 1]), c9), hh, ll);
+            const float2 g23 = __ffma2_rn(make_float2(g[3][u], g[3][u + 1]), c9, make_float2(g[2][u], g[2][u + 1]));
+            ll = __ffma2_rn(g23, c18, ll);
+            const float2 sc = __fmul2_rn(sa2, sb2);  // powers of two: exact
+            hh = __fmul2_rn(hh, sc);
+            ll = __fmul2_rn(ll, sc);
             // acc += (hh, ll); the low word is renormalised by the final update of C (K <= 1024: at most 16 blocks)
-            float s1, t1;
-            two_sum(acc_h[ch * 8 + u], hh, s1, t1);
-            acc_h[ch * 8 + u] = s1;
-            acc_l[ch * 8 + u] = __fadd_rn(acc_l[ch * 8 + u], __fadd_rn(t1, ll));
+            float2 s1, t1;
+            two_sum2(acc_h[cu >> 1], hh, s1, t1);
+            acc_h[cu >> 1] = s1;
+            acc_l[cu >> 1] = __fadd2_rn(acc_l[cu >> 1], __fadd2_rn(t1, ll));
           }
         }
       }
@@ -481,17 +497,18 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int qq = 0; qq < kEpiCols / 4; ++qq) {
           const int off = (((qbase + qq) ^ (r & 7)) << 4);
-          float4 hv = *reinterpret_cast<float4*>(hrow + off), lv = *reinterpret_cast<float4*>(lrow + off);
-          float hx[4] = {hv.x, hv.y, hv.z, hv.w}, lx[4] = {lv.x, lv.y, lv.z, lv.w};
+          const float4 hv = *reinterpret_cast<float4*>(hrow + off), lv = *reinterpret_cast<float4*>(lrow + off);
+          float2 hx[2] = {make_float2(hv.x, hv.y), make_float2(hv.z, hv.w)};
+          float2 lx[2] = {make_float2(lv.x, lv.y), make_float2(lv.z, lv.w)};
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            float sx, tx;
-            two_sum(hx[u], -acc_h[qq * 4 + u], sx, tx);
-            tx = __fadd_rn(tx, __fsub_rn(lx[u], acc_l[qq * 4 + u]));
-            fast_two_sum(sx, tx, hx[u], lx[u]);
+          for (int u = 0; u < 2; ++u) {
+            float2 sx, tx;
+            two_sum2(hx[u], make_float2(-acc_h[qq * 2 + u].x, -acc_h[qq * 2 + u].y), sx, tx);
+            tx = __fadd2_rn(tx, sub2(lx[u], acc_l[qq * 2 + u]));
+            fast_two_sum2(sx, tx, hx[u], lx[u]);
           }
-          *reinterpret_cast<float4*>(hrow + off) = make_float4(hx[0], hx[1], hx[2], hx[3]);
-          *reinterpret_cast<float4*>(lrow + off) = make_float4(lx[0], lx[1], lx[2], lx[3]);
+          *reinterpret_cast<float4*>(hrow + off) = make_float4(hx[0].x, hx[0].y, hx[1].x, hx[1].y);
+          *reinterpret_cast<float4*>(lrow + off) = make_float4(lx[0].x, lx[0].y, lx[1].x, lx[1].y);
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> visible to TMA
@@ -599,7 +616,7 @@ size_t ozaki3_scratch_bytes(int mmax, int ncmax, int Kmax) {
   const size_t Kp = size_t(ceil_div(Kmax, TK)) * TK;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
   return al(kDigits * size_t(mmax) * Kp * 2) + al(kDigits * size_t(ncmax) * Kp * 2) + al(size_t(mmax) * (Kp / TK) * 4) +
-         al(size_t(ncmax) * (Kp / TK) * 4) + 256;
+         al(size_t(ceil_div(ncmax, TN)) * TN * (Kp / TK) * 4) + 256;
 }
 
 int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
