@@ -511,6 +511,20 @@ def gradient(xs, coeffs, centers, kind, param):
     return np.stack([gx, gy], axis=-1)
 
 
+def laplacian(xs, coeffs, centers, kind, param):
+    """Field Laplacian at points ``xs`` (m, 2) (updes/operators.py:319-348): the trace of the Hessian of
+    every kernel term (0 at r = 0) plus the monomials' second derivatives."""
+    xs = np.atleast_2d(xs)
+    N = centers.shape[0]
+    lam, gam = coeffs[:N], coeffs[N:]
+    t = rbf_terms(kind, param, xs[:, 0:1] - centers[None, :, 0], xs[:, 1:2] - centers[None, :, 1])
+    out = np.nan_to_num(lam[None, :] * (t[3] + t[4])).sum(axis=1)
+    for k in range(gam.shape[0]):
+        m = monomial_terms(k, xs[:, 0], xs[:, 1])
+        out = out + gam[k] * (m[3] + m[4])
+    return out
+
+
 def field_coefficients(cloud: Cloud, kind: str, param: float, max_degree: int, values) -> np.ndarray:
     """c = inv(A) [values; 0] (updes/assembly.py:404-430)."""
     A = assemble_A(cloud, kind, param, max_degree)

@@ -184,3 +184,40 @@ def grid_coords(case) -> np.ndarray:
     move = ~np.isin(ftype, ["d", "n", "r"])
     coords[move] += noise[move]
     return coords
+
+
+# --- coupled systems solved with pde_multi_solver (updes/operators.py:686-771) -------------------------
+# Two fields (u, v) on one cloud; every sweep solves each field's PDE with the previous sweep's values of
+# both fields as its leading diff_args, and rhs_args fixed at the old time level.
+#  "grayscott": one implicit step of Gray-Scott reaction-diffusion as in the reference's demo
+#     (demos/Gray-Scott/002_gray_scott_ode.py): operators u and v themselves (nodal_value), right-hand
+#     sides Du Δu_old - u_old v~^2 + F (1 - u_old) and Dv Δv_old + u~ v_old^2 - (F + k) v_old.
+#  "advect": Picard-linearised Burgers (demos/Burgers/00_burgers.py with u u_x written as u~ u_x):
+#     operators u/dt + u~ u_x + v~ u_y and v/dt + u~ v_x + v~ v_y, right-hand sides u_old/dt, v_old/dt.
+GS_DU, GS_DV, GS_F, GS_K = 0.2097, 0.105, 0.03, 0.062
+BURGERS_DT = 0.05
+
+MULTI_CASES = {
+    "multi_grayscott_10x10": dict(Nx=10, Ny=10, facets={"South": "d", "West": "d", "North": "d", "East": "d"},
+                                  rbf=("polyharmonic", 1), max_degree=1, jitter=None, kind="grayscott",
+                                  nb_iters=3),
+    "multi_advect_9x9": dict(Nx=9, Ny=9, facets={"South": "d", "West": "d", "North": "d", "East": "d"},
+                             rbf=("polyharmonic", 1), max_degree=1, jitter=(0.2, 17), kind="advect", nb_iters=4),
+}
+
+
+def multi_initial(case, nodes):
+    """Initial (old-time) values of the two fields at the sorted nodes: smooth bumps, zero on the boundary
+    for the advection case."""
+    x, y = nodes[:, 0], nodes[:, 1]
+    bump = np.exp(-((x - 0.4) ** 2 + (y - 0.55) ** 2) / 0.02)
+    if case["kind"] == "grayscott":
+        return 0.95 - 0.5 * bump, 0.05 + 0.5 * bump
+    s = np.sin(np.pi * x) * np.sin(np.pi * y)
+    return 0.8 * s * (1.0 + 0.5 * bump), 0.4 * s * (1.0 - 0.3 * bump)
+
+
+# --- Gmsh cloud (updes/cloud.py:520-734) on the synthetic mesh written by make_msh.py -----------------
+GMSH_CASE = dict(mesh="dshape.msh", facets={"Bottom": "d", "Right": "n", "Top": "r", "Left": "d"},
+                 rbf=("polyharmonic", 1), max_degree=1, op="laplacian",
+                 bc={"Bottom": "sinsin", "Right": "xy", "Top": ("ylin", "beta2"), "Left": "zero"}, rhs="poisson_rhs")

@@ -9,7 +9,10 @@ For every case in ``cases.CASES`` this builds the reference ``SquareCloud``
 ``pde_solver_jit`` and its assembly functions (``assemble_op_Phi_P``,
 ``assemble_bd_Phi_P``, ``assemble_A``, ``assemble_q``), and stores inputs and
 outputs in ``tests/golden/<case>.npz``.  It also differentiates the reference
-solve (reverse mode, through inv/GEMM/QR) for the boundary-control adjoint case.
+solve (reverse mode, through inv/GEMM/QR) for the boundary-control adjoint case,
+runs the reference's ``pde_multi_solver`` on the two-field cases of
+``cases.MULTI_CASES``, and reads the synthetic mesh of ``make_msh.py`` with the
+reference's ``GmshCloud`` (solving ``cases.GMSH_CASE`` on it).
 """
 from __future__ import annotations
 
@@ -163,13 +166,102 @@ def run_adjoint(updes):
     print("adjoint: J =", float(J))
 
 
+def run_multi(updes, name, case):
+    """The reference's own pde_multi_solver (updes/operators.py:686-771) on a two-field system."""
+    t0 = time.time()
+    coords = C.grid_coords(case)
+
+    class InjectedCloud(updes.SquareCloud):
+        def define_node_coordinates(self, noise_key):
+            self.nodes = {g: torch.tensor(coords[g]) for g in range(self.N)}
+
+    cloud = InjectedCloud(Nx=case["Nx"], Ny=case["Ny"], facet_types=dict(case["facets"]), support_size="max")
+    rbf = partial(updes.polyharmonic, a=int(case["rbf"][1]))
+    if case["kind"] == "grayscott":
+        def dop(x, center=None, rbf=None, monomial=None, fields=None):
+            return updes.nodal_value(x, center, rbf, monomial)
+
+        def rop_u(x, centers=None, rbf=None, fields=None):
+            u_old, v_t = fields[:, 0], fields[:, 1]
+            u, v = updes.value(x, u_old, centers, rbf), updes.value(x, v_t, centers, rbf)
+            return C.GS_DU * updes.laplacian(x, u_old, centers, rbf) - u * v ** 2 + C.GS_F * (1 - u)
+
+        def rop_v(x, centers=None, rbf=None, fields=None):
+            u_t, v_old = fields[:, 0], fields[:, 1]
+            u, v = updes.value(x, u_t, centers, rbf), updes.value(x, v_old, centers, rbf)
+            return C.GS_DV * updes.laplacian(x, v_old, centers, rbf) + u * v ** 2 - (C.GS_F + C.GS_K) * v
+        dops, rops = [dop, dop], [rop_u, rop_v]
+    else:
+        def dop(x, center=None, rbf=None, monomial=None, fields=None):
+            val = updes.nodal_value(x, center, rbf, monomial)
+            grad = updes.nodal_gradient(x, center, rbf, monomial)
+            return val / C.BURGERS_DT + fields[0] * grad[0] + fields[1] * grad[1]
+
+        def rop_u(x, centers=None, rbf=None, fields=None):
+            return updes.value(x, fields[:, 0], centers, rbf) / C.BURGERS_DT
+
+        def rop_v(x, centers=None, rbf=None, fields=None):
+            return updes.value(x, fields[:, 1], centers, rbf) / C.BURGERS_DT
+        dops, rops = [dop, dop], [rop_u, rop_v]
+    zero = lambda c: 0.0 * c[0]
+    bcs = {f: zero for f in case["facets"]}
+    u0, v0 = C.multi_initial(case, np.asarray(cloud.sorted_nodes))
+    prev = [torch.tensor(u0), torch.tensor(v0)]
+    sols = updes.pde_multi_solver(diff_operators=dops, rhs_operators=rops, cloud=cloud,
+                                  boundary_conditions=[dict(bcs), dict(bcs)], rbf=rbf,
+                                  max_degree=case["max_degree"], nb_iters=case["nb_iters"], tol=1e-10,
+                                  diff_args=[list(prev), list(prev)], rhs_args=[list(prev), list(prev)])
+    npy = lambda t: np.asarray(t.detach() if isinstance(t, torch.Tensor) else t, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), case=json.dumps(case), coords=coords,
+                        sorted_nodes=npy(cloud.sorted_nodes), u0=u0, v0=v0,
+                        vals=np.stack([npy(s.vals) for s in sols]), coeffs=np.stack([npy(s.coeffs) for s in sols]))
+    print(f"{name}: N={cloud.N} {time.time() - t0:.1f}s")
+
+
+def run_gmsh(updes):
+    """The reference's GmshCloud on the synthetic mesh and its pde_solver_jit on that cloud."""
+    import jax.numpy as jnp
+    t0 = time.time()
+    case = C.GMSH_CASE
+    cloud = updes.GmshCloud(filename=os.path.join(HERE, case["mesh"]), facet_types=dict(case["facets"]),
+                            support_size="max")
+    rbf = partial(updes.polyharmonic, a=int(case["rbf"][1]))
+
+    def dop(x, center=None, rbf=None, monomial=None, fields=None):
+        return updes.nodal_laplacian(x, center, rbf, monomial)
+
+    def rop(x, centers=None, rbf=None, fields=None):
+        return C.FUNCS[case["rhs"]](jnp, x[0], x[1])
+
+    def bc_fn(name):
+        return lambda coord: C.FUNCS[name](jnp, coord[0], coord[1])
+    bcs = {f: (bc_fn(v[0]), bc_fn(v[1])) if isinstance(v, tuple) else bc_fn(v) for f, v in case["bc"].items()}
+    sol = updes.pde_solver_jit(diff_operator=dop, rhs_operator=rop, cloud=cloud, boundary_conditions=bcs, rbf=rbf,
+                               max_degree=case["max_degree"])
+    npy = lambda t: np.asarray(t.detach() if isinstance(t, torch.Tensor) else t, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "gmsh_dshape.npz"), case=json.dumps(case),
+                        sorted_nodes=npy(cloud.sorted_nodes), sorted_outward_normals=npy(cloud.sorted_outward_normals),
+                        counts=np.array([cloud.N, cloud.Ni, cloud.Nd, cloud.Nn, cloud.Nr], np.int64),
+                        facet_nodes=json.dumps({f: [int(i) for i in v] for f, v in cloud.facet_nodes.items()}),
+                        node_types=json.dumps({int(k): v for k, v in cloud.node_types.items()}),
+                        renumbering=json.dumps({int(k): int(v) for k, v in cloud.renumbering_map.items()}),
+                        vals=npy(sol.vals), coeffs=npy(sol.coeffs))
+    print(f"gmsh_dshape: N={cloud.N} {time.time() - t0:.1f}s")
+
+
 if __name__ == "__main__":
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     updes = load_reference(ref)
-    only = sys.argv[2:] or list(C.CASES)
+    only = sys.argv[2:] or list(C.CASES) + list(C.MULTI_CASES) + ["gmsh"]
     for name in only:
         if name == "adjoint":
             continue
-        run_case(updes, name, C.CASES[name])
+        if name == "gmsh":
+            run_gmsh(updes)
+            continue
+        if name in C.MULTI_CASES:
+            run_multi(updes, name, C.MULTI_CASES[name])
+        else:
+            run_case(updes, name, C.CASES[name])
     if len(sys.argv) <= 2 or "adjoint" in sys.argv[2:]:
         run_adjoint(updes)

@@ -73,8 +73,12 @@ class _AtIndex:
         return out
 
     def add(self, v):
+        idx = self._index()
+        if all(isinstance(i, slice) and i == slice(None) for i in idx):
+            # the whole array: out of place, so that a batched value under vmap broadcasts into the result
+            return self.arr + _t(v).to(self.arr.dtype)
         out = self.arr.clone()
-        out[self._index()] += _t(v).to(out.dtype)
+        out[idx] += _t(v).to(out.dtype)
         return out
 
     def get(self):

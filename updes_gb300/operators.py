@@ -715,6 +715,46 @@ def pde_solver_jit(diff_operator, rhs_operator, cloud, boundary_conditions, rbf,
 pde_solver_jit_with_bc = pde_solver
 
 
+def pde_multi_solver(diff_operators, rhs_operators, cloud, boundary_conditions, rbf, max_degree, nb_iters=10,
+                     tol=1e-6, diff_args=None, rhs_args=None, options=None):
+    """Solve a system of (non-linear) PDEs by Picard sweeps (updes/operators.py:686-771).
+
+    ``diff_operators``, ``rhs_operators`` and ``boundary_conditions`` hold one entry per scalar field.
+    Each of ``nb_iters`` sweeps solves every field's PDE with ``pde_solver``; the first ``n`` diff_args
+    of every PDE are the previous sweep's values of the ``n`` fields (initially ``diff_args[0][:n]``) and
+    the rest of ``diff_args[i]`` and all of ``rhs_args[i]`` stay fixed.  All fields of a sweep see the
+    same previous values (Jacobi order), and the last sweep's ``SteadySol`` list is returned.  As in the
+    reference, ``tol`` does not stop the sweeps early; the relative change of each sweep (the quantity
+    the reference computes) is left in ``LAST_MULTI_INFO["changes"]``.  Fields whose operator weights do
+    not change between solves reuse their factorisation (``SolverOptions.reuse_factorization``).
+    """
+    n = len(diff_operators)
+    if not (n == len(rhs_operators) == len(boundary_conditions)):
+        raise AssertionError("The number of differential operators must match the number of right-hand side "
+                             "operators")
+    if diff_args is None or len(diff_args) < 1 or len(diff_args[0]) < n:
+        raise ValueError("diff_args[0] must start with the initial values of the fields")
+    rhs_args = rhs_args if rhs_args is not None else [None] * n
+    bcs = [boundary_conditions_func_to_arr(b, cloud) for b in boundary_conditions]
+    host = lambda u: u.detach().cpu().numpy() if hasattr(u, "detach") else u
+    vals = [np.asarray(host(u), dtype=np.float64) for u in diff_args[0][:n]]
+    changes = []
+    sols = []
+    for _ in range(int(nb_iters)):
+        sols = [pde_solver(diff_operators[i], rhs_operators[i], cloud, bcs[i], rbf, max_degree,
+                           diff_args=list(vals) + list(diff_args[i][n:]), rhs_args=rhs_args[i], options=options)
+                for i in range(n)]
+        changes.append(float(sum(np.linalg.norm(sols[i].vals - vals[i]) / (np.linalg.norm(vals[i]) + 1e-14)
+                                 for i in range(n))))
+        vals = [s.vals for s in sols]
+    LAST_MULTI_INFO.clear()
+    LAST_MULTI_INFO.update(changes=changes, tol=tol)
+    return sols
+
+
+LAST_MULTI_INFO: dict = {}
+
+
 def materialize_B(dp, cloud, rbf, max_degree):
     """B = K[:N] · inv(A)[:, :N] in FP64 on the GPU (O(n³); diagnostics only)."""
     torch = dp.torch
