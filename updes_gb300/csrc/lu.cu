@@ -1509,6 +1509,243 @@ __global__ void __launch_bounds__(256) trsv_f32_kernel(const float* __restrict__
   }
 }
 
+// Eight-lane version of df_quad_sum (lanes of a row are contiguous: xor 1, 2, 4).
+__device__ __forceinline__ void df_oct_sum(float& h, float& l) {
+#pragma unroll
+  for (int o = 1; o <= 4; o <<= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
+    const float s = __fadd_rn(h, oh);
+    const float bb = __fsub_rn(s, h);
+    float t = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(oh, bb));
+    t = __fadd_rn(t, __fadd_rn(l, ol));
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+  }
+}
+
+// The same triangular solve in blocks of 128 rows, one CTA of 512 threads each: the chain of blocks (an L2
+// hand-off per block) is half as long.  Off-diagonal 128 x 128 tiles are applied as in trsv_f32_kernel
+// (four threads per row, 32 columns each).  The 128 x 128 diagonal block is solved inside the CTA as two
+// 64-row halves with the 64 x 64 inverses of diag_inverse: x_a = D_a r_a, r_b -= T_ba x_a, x_b = D_b r_b
+// (a the half solved first: the upper one going forward, the lower one going backward), eight threads per
+// row.  Same arithmetic (double-float sums of exact FP32 products), same modes.
+constexpr int kTB2 = 2 * kTB;
+constexpr size_t kTrsv128Smem = sizeof(float) * (size_t(kTB2) * (kTB2 + 1) + 4 * size_t(kTB) * (kTB + 1) +
+                                                 size_t(kTB) * (kTB + 1));
+
+template <int MODE>
+__global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restrict__ F, int64_t ldf, int n, double* x,
+                                                          float* xh_g, float* xl_g, int* ticket, int* flags,
+                                                          DeviceStatus* st, const float* __restrict__ dinv) {
+  extern __shared__ __align__(16) unsigned char t128_smem[];
+  float(*sT)[kTB2 + 1] = reinterpret_cast<float(*)[kTB2 + 1]>(t128_smem);
+  float(*sD)[kTB + 1] = reinterpret_cast<float(*)[kTB + 1]>(t128_smem + sizeof(float) * kTB2 * (kTB2 + 1));
+  float(*sC)[kTB + 1] = sD + 4 * kTB;  // the coupling tile T_ba of the diagonal block
+  __shared__ float sxh[kTB2], sxl[kTB2], srh[kTB2], srl[kTB2];
+  __shared__ int s_blk, s_done;
+  const int tid = threadIdx.x;
+  const int nblk = int(ceil_div(n, kTB2));
+  if (tid == 0) {
+    s_blk = atomicAdd(ticket, 1);
+    s_done = 0;
+  }
+  __syncthreads();
+  const int t = s_blk;
+  if (t >= nblk) return;
+  constexpr bool fwd = (MODE == 0 || MODE == 2);
+  constexpr bool trans = (MODE >= 2);
+  const int blk = fwd ? t : nblk - 1 - t;
+  const int r0 = blk * kTB2;
+  const int rows = min(kTB2, n - r0);
+  const int halves = rows > kTB ? 2 : 1;
+  const int first = (fwd || halves == 1) ? 0 : 1, second = 1 - first;  // solve order of the two halves
+  const int row = tid >> 2, part = tid & 3;
+  // inputs no other block writes, fetched before any wait: the right-hand side, both inverse halves and
+  // the coupling tile
+  float bh = 0.f, bl = 0.f;
+  if (part == 0 && row < rows) {
+    const double b = x[r0 + row];
+    bh = float(b);
+    bl = float(b - double(bh));
+  }
+  {
+    constexpr int which = (MODE == 0 || MODE == 3) ? 0 : 1;  // 0: inv(L_bb), 1: inv(U_bb); transposed for 2, 3
+    for (int hlf = 0; hlf < halves; ++hlf) {
+      const int bb = 2 * blk + hlf;  // 64-row block of diag_inverse
+      const float* Dh = dinv + (size_t(bb) * 4 + which * 2) * kTB * kTB;
+      const float* Dlo = Dh + kTB * kTB;
+      for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+        const int a = e >> 6, b = e & 63;
+        const int ra = trans ? b : a, cb = trans ? a : b;
+        sD[(2 * hlf) * kTB + ra][cb] = __ldg(Dh + e);
+        sD[(2 * hlf + 1) * kTB + ra][cb] = __ldg(Dlo + e);
+      }
+    }
+  }
+  float cpre[8];
+  if (halves == 2) {
+    // T_ba(i, j) = op(r0 + 64 second + i, r0 + 64 first + j); read row-contiguously, stored as [i][j]
+    const int rs = r0 + kTB * second, cs = r0 + kTB * first;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = tid + 512 * i;
+      const int a = e >> 6, b = e & 63;
+      float v = 0.f;  // rows and columns past n (a partial last block) are zero
+      if (!trans) {
+        if (rs + a < n && cs + b < n) v = F[int64_t(rs + a) * ldf + cs + b];
+      } else {
+        if (cs + a < n && rs + b < n) v = F[int64_t(cs + a) * ldf + rs + b];
+      }
+      cpre[i] = v;
+    }
+  }
+  auto load_tile = [&](int c0, float (&pre)[32]) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int e = tid + 512 * i;
+      const int a = e >> 7, b = e & 127;
+      float v = 0.f;
+      if (!trans) {
+        if (r0 + a < n && c0 + b < n) v = F[int64_t(r0 + a) * ldf + c0 + b];
+      } else {
+        if (c0 + a < n && r0 + b < n) v = F[int64_t(c0 + a) * ldf + r0 + b];
+      }
+      pre[i] = v;
+    }
+  };
+  float pre[32];
+  if (t > 0) load_tile((fwd ? 0 : nblk - 1) * kTB2, pre);
+  float ah = 0.f, al = 0.f;
+  for (int q = 0; q < t; ++q) {
+    const int jb = fwd ? q : nblk - 1 - q;
+    const int c0 = jb * kTB2;
+    const int cols = min(kTB2, n - c0);
+    if (tid == 0 && s_done <= q) {
+      volatile int* vc = flags + nblk;
+      long long it = 0;
+      int d;
+      while ((d = *vc) <= q) {
+        if (++it > kSpinLimit) {
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, 30 + MODE);
+          d = q + 1;
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+      s_done = d;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int e = tid + 512 * i;
+      const int a = e >> 7, b = e & 127;
+      if (!trans) sT[a][b] = pre[i];
+      else sT[b][a] = pre[i];
+    }
+    if (tid < kTB2) {
+      sxh[tid] = tid < cols ? __ldcg(xh_g + c0 + tid) : 0.f;
+      sxl[tid] = tid < cols ? __ldcg(xl_g + c0 + tid) : 0.f;
+    }
+    __syncthreads();
+    if (q + 1 < t) load_tile((fwd ? q + 1 : nblk - 2 - q) * kTB2, pre);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const int c = part * 32 + ((k + 8 * part) & 31);  // rotated per part: no bank conflicts
+      df_fma(sT[row][c], sxh[c], sxl[c], ah, al);
+    }
+    __syncthreads();
+  }
+  df_quad_sum(ah, al);
+  if (part == 0) {
+    // right-hand side of this block minus the off-diagonal part, double-float
+    float rh = 0.f, rl = 0.f;
+    if (row < rows) {
+      const float ch = -ah, cl = -al;
+      const float s0 = __fadd_rn(bh, ch);
+      const float bb = __fsub_rn(s0, bh);
+      float tt = __fadd_rn(__fsub_rn(bh, __fsub_rn(s0, bb)), __fsub_rn(ch, bb));
+      tt = __fadd_rn(tt, __fadd_rn(bl, cl));
+      rh = __fadd_rn(s0, tt);
+      rl = __fsub_rn(tt, __fsub_rn(rh, s0));
+    }
+    srh[row] = rh;
+    srl[row] = rl;
+  }
+  if (halves == 2) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = tid + 512 * i;
+      const int a = e >> 6, b = e & 63;
+      if (!trans) sC[a][b] = cpre[i];
+      else sC[b][a] = cpre[i];
+    }
+  }
+  __syncthreads();
+  // the diagonal block, eight threads per row of a 64-row half
+  const int drow = tid >> 3, dpart = tid & 7;
+  auto solve_half = [&](int hlf) {  // x = D_hlf r_hlf into (srh, srl) of that half, in place after a barrier
+    float ph = 0.f, pl = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int c = dpart * 8 + ((k + drow) & 7);
+      const float dh = sD[(2 * hlf) * kTB + drow][c], dl = sD[(2 * hlf + 1) * kTB + drow][c];
+      const float xh = srh[kTB * hlf + c], xl = srl[kTB * hlf + c];
+      const float p = __fmul_rn(dh, xh);
+      const float pe = __fmaf_rn(dh, xh, -p);
+      const float s0 = __fadd_rn(ph, p);
+      const float bb = __fsub_rn(s0, ph);
+      float tt = __fadd_rn(__fsub_rn(ph, __fsub_rn(s0, bb)), __fsub_rn(p, bb));
+      tt = __fadd_rn(tt, __fadd_rn(pl, __fmaf_rn(dh, xl, __fmaf_rn(dl, xh, pe))));
+      ph = __fadd_rn(s0, tt);
+      pl = __fsub_rn(tt, __fsub_rn(ph, s0));
+    }
+    df_oct_sum(ph, pl);
+    __syncthreads();  // every thread has read r of this half
+    if (dpart == 0) {
+      srh[kTB * hlf + drow] = ph;
+      srl[kTB * hlf + drow] = pl;
+    }
+    __syncthreads();
+  };
+  solve_half(first);
+  if (halves == 2) {
+    // r_second -= T x_first
+    float ah2 = 0.f, al2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int c = dpart * 8 + ((k + drow) & 7);
+      df_fma(sC[drow][c], srh[kTB * first + c], srl[kTB * first + c], ah2, al2);
+    }
+    df_oct_sum(ah2, al2);
+    if (dpart == 0) {
+      const int i = kTB * second + drow;
+      const float ch = -ah2, cl = -al2, rh0 = srh[i], rl0 = srl[i];
+      const float s0 = __fadd_rn(rh0, ch);
+      const float bb = __fsub_rn(s0, rh0);
+      float tt = __fadd_rn(__fsub_rn(rh0, __fsub_rn(s0, bb)), __fsub_rn(ch, bb));
+      tt = __fadd_rn(tt, __fadd_rn(rl0, cl));
+      const float nh = __fadd_rn(s0, tt);
+      srh[i] = nh;
+      srl[i] = __fsub_rn(tt, __fsub_rn(nh, s0));
+    }
+    __syncthreads();
+    solve_half(second);
+  }
+  if (tid < rows) {
+    const float ph = srh[tid], pl = srl[tid];
+    xh_g[r0 + tid] = ph;
+    xl_g[r0 + tid] = pl;
+    x[r0 + tid] = double(ph) + double(pl);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    atomicAdd(flags + nblk, 1);  // blocks finish in order: this is block number t
+  }
+}
+
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
               const float* dinv, float* xh, float* xl) {
@@ -1520,6 +1757,29 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
   if (sizeof(TF) != 4) dinv = nullptr;
   if constexpr (sizeof(TF) == 4) {
     if (dinv && xh && xl) {
+      // UPDES_TRSV_BLOCK=64 selects the 64-row kernel
+      static const bool rows128 = [] {
+        const char* v = std::getenv("UPDES_TRSV_BLOCK");
+        return !(v && std::atoi(v) == 64);
+      }();
+      if (rows128) {
+        static std::atomic<unsigned long long> attr128[4] = {};
+        int e;
+        if ((e = smem_opt_in((const void*)trsv128_f32_kernel<0>, int(kTrsv128Smem), attr128[0])) ||
+            (e = smem_opt_in((const void*)trsv128_f32_kernel<1>, int(kTrsv128Smem), attr128[1])) ||
+            (e = smem_opt_in((const void*)trsv128_f32_kernel<2>, int(kTrsv128Smem), attr128[2])) ||
+            (e = smem_opt_in((const void*)trsv128_f32_kernel<3>, int(kTrsv128Smem), attr128[3])))
+          return e;
+        const unsigned g = unsigned(ceil_div(n, kTB2));
+        switch (mode) {
+          case 0: trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+          case 1: trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+          case 2: trsv128_f32_kernel<2><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+          default: trsv128_f32_kernel<3><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+        }
+        UPDES_LAUNCH_CHECK();
+        return UPDES_OK;
+      }
       const size_t smem = 2 * sizeof(float) * kTB * (kTB + 1);
       static std::atomic<unsigned long long> attr[4] = {};
       int e;
