@@ -39,7 +39,7 @@ for n in {sizes!r}:
     print(n, info.value, h)
 """
 
-SIZES = [1024, 1300, 2113]
+SIZES = [1024, 1300, 2113, 12600]  # 12600: the first steps fork after the whole block row, the later ones early
 
 
 def _digests(lookahead):

@@ -762,6 +762,11 @@ constexpr int kOuterNb = 4 * kLuNb;   // 256: width of the big exact trailing up
 constexpr int kSwapMapInts = 512;     // one panel's swap map (257 ints used): 2 KB per slot
 constexpr int kLookaheadMinN = 1024;  // smaller factorisations run their steps in order on one stream
 constexpr int kLookaheadCtas = kMaxPanelCtas;  // SMs kept for the look-ahead block beside the trailing update
+// Below this many trailing rows the next block's factorisation (linear in the rows) outlasts the trailing
+// update (quadratic): the side stream then forks as soon as the next block's own columns are ready, and the
+// rest of the step's interchanges and U row follow beside it.  Above it they stay before the fork, on all
+// SMs, where they shorten the update stream that bounds the step.
+constexpr int kEarlyForkRows = 12288;
 
 size_t lu_df_workspace_bytes(int n) {
   // panel scratch (rounded up to 256 B), the swap maps of one 256-column block's panels, the digit scratch of
@@ -928,25 +933,26 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     }
     return UPDES_OK;
   };
-  // The deferred interchanges of block [K0, KE) on the columns outside it, panel by panel.
-  auto swaps_outside = [&](int K0, int KE) -> int {
+  // The deferred interchanges of block [K0, KE), panel by panel, on trailing columns [c0, c1) (both planes)
+  // and, with left, on the factored columns [0, K0) (the FP32 factors).
+  auto swaps_deferred = [&](int K0, int KE, int c0, int c1, bool left) -> int {
     for (int k = K0, p = 0; k < KE; k += nb, ++p) {
       SwapJobs j{};
       int64_t maxc = 0;
-      add_swap_job(j, maxc, Whi, 0, K0);
-      add_swap_job(j, maxc, Whi, KE, n);
-      add_swap_job(j, maxc, Wlo, KE, n);
+      if (left) add_swap_job(j, maxc, Whi, 0, K0);
+      add_swap_job(j, maxc, Whi, c0, c1);
+      add_swap_job(j, maxc, Wlo, c0, c1);
       if (int e = swap_launch(j, maxc, swap_maps + p * kSwapMapInts, s)) return e;
     }
     return UPDES_OK;
   };
-  // Block row of U for block [K0, KE) on the trailing columns [KE, n).
-  auto block_row = [&](int K0, int KE) -> int {
+  // Block row of U for block [K0, KE) on trailing columns [c0, c1), the updates on at most ctas CTAs.
+  auto block_row = [&](int K0, int KE, int c0, int c1, int ctas) -> int {
     for (int b = K0; b < KE; b += nb) {
       const int w = std::min(nb, KE - b);
-      if (int e = trsm(b, w, KE, n, s)) return e;
+      if (int e = trsm(b, w, c0, c1, s)) return e;
       if (b + w < KE)
-        if (int e = upd(b + w, KE, KE, n, b, b + w, s, digits, digits_bytes, 0)) return e;
+        if (int e = upd(b + w, KE, c0, c1, b, b + w, s, digits, digits_bytes, ctas)) return e;
     }
     return UPDES_OK;
   };
@@ -954,22 +960,39 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   SideStream side;
   int e;
   if (lookahead && (e = side.create(s))) return e;
+  const int rest_ctas = std::max(num_sms() - kLookaheadCtas, num_sms() / 2);
+  // UPDES_EARLY_FORK_ROWS overrides kEarlyForkRows (same factors either way)
+  static const int early_rows = [] {
+    const char* v = std::getenv("UPDES_EARLY_FORK_ROWS");
+    return v ? std::atoi(v) : kEarlyForkRows;
+  }();
   int K0 = 0, KE = std::min(kOuter, n);
   if ((e = factor_block(K0, KE, false, s, 0))) return e;
+  bool pending = false;  // block [K0, KE) was factored beside the update: its outside interchanges are due
   while (KE < n) {
     const int KE2 = std::min(KE + kOuter, n);
-    if ((e = block_row(K0, KE))) return e;
-    if ((e = upd(KE, n, KE, KE2, K0, KE, s, digits, digits_bytes, 0))) return e;  // the next block's columns
+    const bool early_fork = lookahead && KE2 < n && n - KE <= early_rows;
+    // what the next block [KE, KE2) needs before it can be factored: this block's interchanges, U row and
+    // update on its columns (with an early fork), or on all trailing columns
+    const int c1 = early_fork ? KE2 : n;
+    if (pending && (e = swaps_deferred(K0, KE, KE, c1, !early_fork))) return e;
+    if ((e = block_row(K0, KE, KE, c1, 0))) return e;
+    if ((e = upd(KE, n, KE, KE2, K0, KE, s, digits, digits_bytes, 0))) return e;
     if (lookahead && KE2 < n) {
+      // the next block on the side stream; the rest of this step on this stream, on the SMs it leaves
       if ((e = side.start())) return e;
       if ((e = factor_block(KE, KE2, true, side.side, kLookaheadCtas))) return e;
-      const int rest_ctas = std::max(num_sms() - kLookaheadCtas, num_sms() / 2);
+      if (early_fork) {
+        if (pending && (e = swaps_deferred(K0, KE, KE2, n, true))) return e;
+        if ((e = block_row(K0, KE, KE2, n, rest_ctas))) return e;
+      }
       if ((e = upd(KE, n, KE2, n, K0, KE, s, digits, digits_bytes, rest_ctas))) return e;
       if ((e = side.finish())) return e;
-      if ((e = swaps_outside(KE, KE2))) return e;
+      pending = true;
     } else {
       if (KE2 < n && (e = upd(KE, n, KE2, n, K0, KE, s, digits, digits_bytes, 0))) return e;
       if ((e = factor_block(KE, KE2, false, s, 0))) return e;
+      pending = false;
     }
     K0 = KE;
     KE = KE2;

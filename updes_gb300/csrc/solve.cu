@@ -110,8 +110,22 @@ __global__ void col_max_f32_kernel(const float* __restrict__ Khi, int64_t ld, in
   if (j >= n) return;
   const int rows = int(ceil_div(n, kColScaleChunks));
   const int i0 = blockIdx.y * rows, i1 = min(n, i0 + rows);
-  double m = 0.0;
-  for (int i = i0; i < i1; ++i) m = fmax(m, double(fabsf(Khi[int64_t(i) * ld + j])) * dr[i]);
+  // eight independent loads in flight per thread (the column walk is otherwise one dependent load per row);
+  // |hi| dr_i is formed in FP32 (dr is a power of two, exact) and widened once at the end
+  float m8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  int i = i0;
+  for (; i + 8 <= i1; i += 8) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(Khi + int64_t(i + u) * ld + j);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) m8[u] = fmaxf(m8[u], fabsf(v[u]) * float(dr[i + u]));
+  }
+  for (; i < i1; ++i) m8[0] = fmaxf(m8[0], fabsf(__ldg(Khi + int64_t(i) * ld + j)) * float(dr[i]));
+  float mf = m8[0];
+#pragma unroll
+  for (int u = 1; u < 8; ++u) mf = fmaxf(mf, m8[u]);
+  const double m = double(mf);
   if (m > 0.0) atomicMax(colmax + j, (unsigned long long)__double_as_longlong(m));
 }
 
