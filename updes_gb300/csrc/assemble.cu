@@ -224,6 +224,80 @@ __global__ void __launch_bounds__(256) eval_values_kernel(updes_problem p, const
   }
 }
 
+// vals = [Phi P] c with the symmetry of Phi (phi(x_i - x_j) = phi(x_j - x_i)): every kernel value of a
+// 64 x 64 tile pair (I, J), I < J, serves row i of block I (phi_ij c_j) and row j of block J (phi_ij c_i),
+// so half the FP64 evaluations of eval_values_kernel.  part[b * N + i] receives the sum over block b's
+// columns for row i, written exactly once (by tile (I, b) when b >= I, as the column sum of tile (b, I)
+// otherwise); eval_values_sym_reduce adds the blocks in order, so the result is deterministic.
+constexpr int kSymT = 64;
+
+template <int KIND>
+__global__ void __launch_bounds__(256) eval_values_sym_kernel(updes_problem p, const double* __restrict__ coeffs,
+                                                              double* __restrict__ part) {
+  const int J = blockIdx.x, I = blockIdx.y;
+  if (I > J) return;
+  __shared__ double scol[16][kSymT + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int N = p.N;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int i0 = I * kSymT + ty * 4, j0 = J * kSymT + tx * 4;
+  double xi[4], yi[4], ci[4], xj[4], yj[4], cj[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = min(i0 + u, N - 1), j = min(j0 + u, N - 1);
+    xi[u] = p.nodes[2 * i];
+    yi[u] = p.nodes[2 * i + 1];
+    ci[u] = i0 + u < N ? coeffs[i] : 0.0;
+    xj[u] = p.nodes[2 * j];
+    yj[u] = p.nodes[2 * j + 1];
+    cj[u] = j0 + u < N ? coeffs[j] : 0.0;
+  }
+  double racc[4] = {0.0, 0.0, 0.0, 0.0}, cacc[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool diag = (I == J);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (diag && i0 + u == j0 + v && !p.self_term) continue;
+      const double phi = rbf_value<KIND>(xi[u] - xj[v], yi[u] - yj[v], p.rbf_param, ip);
+      racc[u] = fma(phi, cj[v], racc[u]);   // padding columns carry c = 0
+      cacc[v] = fma(phi, ci[u], cacc[v]);   // padding rows carry c = 0
+    }
+  }
+  // row sums over the tile's 64 columns: the 16 lanes of a row group (xor 1..8 stay inside the group)
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    for (int o = 8; o > 0; o >>= 1) racc[u] += __shfl_xor_sync(0xffffffffu, racc[u], o);
+  if (tx == 0)
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u < N) part[int64_t(J) * N + i0 + u] = racc[u];
+  if (!diag) {
+    // column sums over the tile's 64 rows, through shared memory (the 16 row groups span warps)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) scol[ty][tx * 4 + v] = cacc[v];
+    __syncthreads();
+    if (tid < kSymT) {
+      double sum = 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) sum += scol[q][tid];
+      const int j = J * kSymT + tid;
+      if (j < N) part[int64_t(I) * N + j] = sum;
+    }
+  }
+}
+
+__global__ void eval_values_sym_reduce(updes_problem p, const double* __restrict__ part, int nblk,
+                                       const double* __restrict__ coeffs, double* __restrict__ vals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += part[int64_t(b) * p.N + i];
+  const double x = p.nodes[2 * i], y = p.nodes[2 * i + 1];
+  for (int k = 0; k < p.M; ++k) s += monomial_terms(k, x, y).m * coeffs[p.N + k];
+  vals[i] = s;
+}
+
 // Field at arbitrary points from coefficients, summing over every center
 // (updes/operators.py:118-184 value / gradient, :319-348 laplacian).
 // what: 0 value (out m), 1 gradient (out m x 2), 2 laplacian (out m).
@@ -694,6 +768,28 @@ extern "C" int updes_assemble_df(const updes_problem* p, float* Khi, float* Klo,
   dim3 block(32, kAsmWarps);
   dim3 grid(unsigned(ceil_div(ld, kAsmCols)), unsigned(ceil_div(n, kAsmRows)));
   assemble_df_kernel<<<grid, block, 0, s>>>(*p, n, rows, tri, Khi, Klo, ld, rowmax, range_flag);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
+
+size_t eval_values_sym_bytes(int N) { return size_t(ceil_div(N, kSymT)) * size_t(N) * sizeof(double); }
+
+// updes_eval_values through the symmetric kernel, with a scratch of eval_values_sym_bytes(N) bytes.
+int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, double* part, cudaStream_t s) {
+  int st = check_problem(p);
+  if (st) return st;
+  if (!coeffs || !vals || !part) return UPDES_ERR_INVALID;
+  const int nblk = int(ceil_div(p->N, kSymT));
+  const dim3 grid{unsigned(nblk), unsigned(nblk)};
+  switch (p->rbf) {
+    case UPDES_RBF_POLYHARMONIC: eval_values_sym_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, coeffs, part); break;
+    case UPDES_RBF_GAUSSIAN: eval_values_sym_kernel<UPDES_RBF_GAUSSIAN><<<grid, 256, 0, s>>>(*p, coeffs, part); break;
+    case UPDES_RBF_MULTIQUADRIC: eval_values_sym_kernel<UPDES_RBF_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, coeffs, part); break;
+    case UPDES_RBF_INVERSE_MULTIQUADRIC: eval_values_sym_kernel<UPDES_RBF_INVERSE_MULTIQUADRIC><<<grid, 256, 0, s>>>(*p, coeffs, part); break;
+    default: eval_values_sym_kernel<UPDES_RBF_THIN_PLATE><<<grid, 256, 0, s>>>(*p, coeffs, part); break;
+  }
+  UPDES_LAUNCH_CHECK();
+  eval_values_sym_reduce<<<unsigned(ceil_div(p->N, 256)), 256, 0, s>>>(*p, part, nblk, coeffs, vals);
   UPDES_LAUNCH_CHECK();
   return UPDES_OK;
 }

@@ -19,6 +19,8 @@
 #include "stats.cuh"
 
 int updes_check_problem(const updes_problem* p);
+size_t eval_values_sym_bytes(int N);
+int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, double* part, cudaStream_t s);
 
 namespace {
 
@@ -652,6 +654,7 @@ namespace {
 struct SolveWs {
   LuWs lu;
   double *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *partial, *h;
+  double* evp;  // per-tile partial sums of the symmetric value evaluation
   float *Khi, *Klo;  // equilibrated K as double-float planes (kept for the refinement's residuals)
   float *xh, *xl;    // FP32 planes of the vector a GEMV multiplies
   float* F32;  // hi plane = FP32 factors
@@ -680,6 +683,7 @@ size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* ou
   w.piv = c.take<int32_t>(2 * size_t(n));
   w.state = c.take<int32_t>(64);
   w.dinv = c.take<float>(diag_inverse_bytes(n) / sizeof(float));
+  w.evp = c.take<double>(eval_values_sym_bytes(n) / sizeof(double));
   w.dr = c.take<double>(n);
   w.dc = c.take<double>(n);
   w.bs = c.take<double>(n);
@@ -1089,12 +1093,12 @@ int solve_stage(const updes_problem* p, const SolveWs& w, int n, const double* q
   UPDES_LAUNCH_CHECK();
   if (cstride == 1) {
     UPDES_CUDA_TRY(cudaMemcpyAsync(coeffs, w.x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    if (vals && vstride == 1 && (e = updes_eval_values(p, coeffs, vals, s))) return e;
+    if (vals && vstride == 1 && (e = eval_values_sym(p, coeffs, vals, w.evp, s))) return e;
   } else {
     UPDES_CUDA_TRY(cudaMemcpy2DAsync(coeffs, cstride * 8, w.x, 8, 8, n, cudaMemcpyDeviceToDevice, s));
   }
   if (vals && (cstride != 1 || vstride != 1)) {
-    if ((e = updes_eval_values(p, w.x, w.wv, s))) return e;
+    if ((e = eval_values_sym(p, w.x, w.wv, w.evp, s))) return e;
     UPDES_CUDA_TRY(cudaMemcpy2DAsync(vals, vstride * 8, w.wv, 8, 8, p->N, cudaMemcpyDeviceToDevice, s));
   }
   info->t_eval_ms += t.stop();
