@@ -1532,39 +1532,49 @@ __global__ void __launch_bounds__(256) trsv_f32_kernel(const float* __restrict__
   }
 }
 
-// Eight-lane version of df_quad_sum (lanes of a row are contiguous: xor 1, 2, 4).
-__device__ __forceinline__ void df_oct_sum(float& h, float& l) {
-#pragma unroll
-  for (int o = 1; o <= 4; o <<= 1) {
-    const float oh = __shfl_xor_sync(0xffffffffu, h, o), ol = __shfl_xor_sync(0xffffffffu, l, o);
-    const float s = __fadd_rn(h, oh);
-    const float bb = __fsub_rn(s, h);
-    float t = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(oh, bb));
-    t = __fadd_rn(t, __fadd_rn(l, ol));
-    h = __fadd_rn(s, t);
-    l = __fsub_rn(t, __fsub_rn(h, s));
-  }
+// (ah, al) += (bh, bl), renormalised.
+__device__ __forceinline__ void df_add_to(float& ah, float& al, float bh, float bl) {
+  const float s0 = __fadd_rn(ah, bh);
+  const float bb = __fsub_rn(s0, ah);
+  float t = __fadd_rn(__fsub_rn(ah, __fsub_rn(s0, bb)), __fsub_rn(bh, bb));
+  t = __fadd_rn(t, __fadd_rn(al, bl));
+  ah = __fadd_rn(s0, t);
+  al = __fsub_rn(t, __fsub_rn(ah, s0));
+}
+
+// df_fma on two independent column pairs at once with the packed FP32x2 instructions of sm_100+ (one
+// issue slot per pair); y - x is fma(x, -1, y), which rounds once like a subtraction.
+__device__ __forceinline__ float2 sub2(float2 y, float2 x) { return __ffma2_rn(x, make_float2(-1.f, -1.f), y); }
+
+__device__ __forceinline__ void df_fma_x2(float2 f, float2 fl, float2 xh, float2 xl, float2& sh, float2& sl) {
+  const float2 p = __fmul2_rn(f, xh);
+  const float2 pe = __ffma2_rn(f, xh, make_float2(-p.x, -p.y));
+  const float2 s0 = __fadd2_rn(sh, p);
+  const float2 bb = sub2(s0, sh);
+  float2 t = __fadd2_rn(sub2(sh, sub2(s0, bb)), sub2(p, bb));
+  t = __fadd2_rn(t, __fadd2_rn(sl, __ffma2_rn(f, xl, __ffma2_rn(fl, xh, pe))));
+  sh = __fadd2_rn(s0, t);
+  sl = sub2(t, sub2(sh, s0));
 }
 
 // The same triangular solve in blocks of 128 rows, one CTA of 512 threads each: the chain of blocks (an L2
 // hand-off per block) is half as long.  Off-diagonal 128 x 128 tiles are applied as in trsv_f32_kernel
-// (four threads per row, 32 columns each).  The 128 x 128 diagonal block is solved inside the CTA as two
-// 64-row halves with the 64 x 64 inverses of diag_inverse: x_a = D_a r_a, r_b -= T_ba x_a, x_b = D_b r_b
-// (a the half solved first: the upper one going forward, the lower one going backward), eight threads per
-// row.  Same arithmetic (double-float sums of exact FP32 products), same modes.
+// (four threads per row, 32 columns each, two independent accumulators); each prefetched tile is stored to
+// shared memory before its block's flag is awaited, so that only the solved x and the arithmetic follow
+// the flag.  The diagonal block is one matrix-vector product with its inverse (diag_inverse128).
 constexpr int kTB2 = 2 * kTB;
-constexpr size_t kTrsv128Smem = sizeof(float) * (size_t(kTB2) * (kTB2 + 1) + 4 * size_t(kTB) * (kTB + 1) +
-                                                 size_t(kTB) * (kTB + 1));
+constexpr int kT2S = kTB2 + 2;  // even row stride: column pairs load as aligned 8-byte vectors
+constexpr size_t kTrsv128Smem = sizeof(float) * 3 * size_t(kTB2) * kT2S;
 
 template <int MODE>
 __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restrict__ F, int64_t ldf, int n, double* x,
                                                           float* xh_g, float* xl_g, int* ticket, int* flags,
-                                                          DeviceStatus* st, const float* __restrict__ dinv) {
+                                                          DeviceStatus* st, const float* __restrict__ dinv128) {
   extern __shared__ __align__(16) unsigned char t128_smem[];
-  float(*sT)[kTB2 + 1] = reinterpret_cast<float(*)[kTB2 + 1]>(t128_smem);
-  float(*sD)[kTB + 1] = reinterpret_cast<float(*)[kTB + 1]>(t128_smem + sizeof(float) * kTB2 * (kTB2 + 1));
-  float(*sC)[kTB + 1] = sD + 4 * kTB;  // the coupling tile T_ba of the diagonal block
-  __shared__ float sxh[kTB2], sxl[kTB2], srh[kTB2], srl[kTB2];
+  float(*sT)[kT2S] = reinterpret_cast<float(*)[kT2S]>(t128_smem);
+  float(*sDh)[kT2S] = sT + kTB2;
+  float(*sDl)[kT2S] = sDh + kTB2;
+  __shared__ __align__(8) float sxh[kTB2], sxl[kTB2], srh[kTB2], srl[kTB2];
   __shared__ int s_blk, s_done;
   const int tid = threadIdx.x;
   const int nblk = int(ceil_div(n, kTB2));
@@ -1580,11 +1590,8 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
   const int blk = fwd ? t : nblk - 1 - t;
   const int r0 = blk * kTB2;
   const int rows = min(kTB2, n - r0);
-  const int halves = rows > kTB ? 2 : 1;
-  const int first = (fwd || halves == 1) ? 0 : 1, second = 1 - first;  // solve order of the two halves
   const int row = tid >> 2, part = tid & 3;
-  // inputs no other block writes, fetched before any wait: the right-hand side, both inverse halves and
-  // the coupling tile
+  // inputs no other block writes, fetched before any wait: the right-hand side and the inverse block
   float bh = 0.f, bl = 0.f;
   if (part == 0 && row < rows) {
     const double b = x[r0 + row];
@@ -1593,33 +1600,13 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
   }
   {
     constexpr int which = (MODE == 0 || MODE == 3) ? 0 : 1;  // 0: inv(L_bb), 1: inv(U_bb); transposed for 2, 3
-    for (int hlf = 0; hlf < halves; ++hlf) {
-      const int bb = 2 * blk + hlf;  // 64-row block of diag_inverse
-      const float* Dh = dinv + (size_t(bb) * 4 + which * 2) * kTB * kTB;
-      const float* Dlo = Dh + kTB * kTB;
-      for (int e = tid; e < kTB * kTB; e += blockDim.x) {
-        const int a = e >> 6, b = e & 63;
-        const int ra = trans ? b : a, cb = trans ? a : b;
-        sD[(2 * hlf) * kTB + ra][cb] = __ldg(Dh + e);
-        sD[(2 * hlf + 1) * kTB + ra][cb] = __ldg(Dlo + e);
-      }
-    }
-  }
-  float cpre[8];
-  if (halves == 2) {
-    // T_ba(i, j) = op(r0 + 64 second + i, r0 + 64 first + j); read row-contiguously, stored as [i][j]
-    const int rs = r0 + kTB * second, cs = r0 + kTB * first;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int e = tid + 512 * i;
-      const int a = e >> 6, b = e & 63;
-      float v = 0.f;  // rows and columns past n (a partial last block) are zero
-      if (!trans) {
-        if (rs + a < n && cs + b < n) v = F[int64_t(rs + a) * ldf + cs + b];
-      } else {
-        if (cs + a < n && rs + b < n) v = F[int64_t(cs + a) * ldf + rs + b];
-      }
-      cpre[i] = v;
+    const float* Dh = dinv128 + (size_t(blk) * 2 + which) * 2 * kTB2 * kTB2;
+    const float* Dlo = Dh + kTB2 * kTB2;
+    for (int e = tid; e < kTB2 * kTB2; e += blockDim.x) {
+      const int a = e >> 7, b = e & 127;
+      const int ra = trans ? b : a, cb = trans ? a : b;
+      sDh[ra][cb] = __ldg(Dh + e);
+      sDl[ra][cb] = __ldg(Dlo + e);
     }
   }
   auto load_tile = [&](int c0, float (&pre)[32]) {
@@ -1636,12 +1623,27 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
       pre[i] = v;
     }
   };
+  auto store_tile = [&](const float (&pre)[32]) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+      const int e = tid + 512 * i;
+      const int a = e >> 7, b = e & 127;
+      if (!trans) sT[a][b] = pre[i];
+      else sT[b][a] = pre[i];
+    }
+  };
+  auto tile_cols = [&](int q) { return (fwd ? q : nblk - 1 - q) * kTB2; };
   float pre[32];
-  if (t > 0) load_tile((fwd ? 0 : nblk - 1) * kTB2, pre);
-  float ah = 0.f, al = 0.f;
+  if (t > 0) {
+    load_tile(tile_cols(0), pre);
+    store_tile(pre);
+    if (t > 1) load_tile(tile_cols(1), pre);
+  }
+  // two accumulators (even and odd columns of a pair) on packed pairs: half the dependent chain and half the
+  // instructions
+  float2 acc_h = make_float2(0.f, 0.f), acc_l = make_float2(0.f, 0.f);
   for (int q = 0; q < t; ++q) {
-    const int jb = fwd ? q : nblk - 1 - q;
-    const int c0 = jb * kTB2;
+    const int c0 = tile_cols(q);
     const int cols = min(kTB2, n - c0);
     if (tid == 0 && s_done <= q) {
       volatile int* vc = flags + nblk;
@@ -1659,108 +1661,55 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
       __threadfence();
       s_done = d;
     }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const int e = tid + 512 * i;
-      const int a = e >> 7, b = e & 127;
-      if (!trans) sT[a][b] = pre[i];
-      else sT[b][a] = pre[i];
-    }
+    __syncthreads();  // tile q is in sT (stored in the previous round); block q is solved
     if (tid < kTB2) {
       sxh[tid] = tid < cols ? __ldcg(xh_g + c0 + tid) : 0.f;
       sxl[tid] = tid < cols ? __ldcg(xl_g + c0 + tid) : 0.f;
     }
     __syncthreads();
-    if (q + 1 < t) load_tile((fwd ? q + 1 : nblk - 2 - q) * kTB2, pre);
 #pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      const int c = part * 32 + ((k + 8 * part) & 31);  // rotated per part: no bank conflicts
-      df_fma(sT[row][c], sxh[c], sxl[c], ah, al);
+    for (int k = 0; k < 16; ++k) {
+      const int c = part * 32 + 2 * ((k + 4 * part) & 15);  // column pair, rotated per part
+      const float2 f = *reinterpret_cast<const float2*>(&sT[row][c]);
+      df_fma_x2(f, make_float2(0.f, 0.f), *reinterpret_cast<const float2*>(&sxh[c]),
+                *reinterpret_cast<const float2*>(&sxl[c]), acc_h, acc_l);
     }
-    __syncthreads();
+    __syncthreads();  // every thread is done with sT and sx
+    if (q + 1 < t) {
+      store_tile(pre);  // tile q + 1, before its block's flag is awaited
+      if (q + 2 < t) load_tile(tile_cols(q + 2), pre);
+    }
   }
+  float ah = acc_h.x, al = acc_l.x;
+  df_add_to(ah, al, acc_h.y, acc_l.y);
   df_quad_sum(ah, al);
   if (part == 0) {
     // right-hand side of this block minus the off-diagonal part, double-float
     float rh = 0.f, rl = 0.f;
     if (row < rows) {
-      const float ch = -ah, cl = -al;
-      const float s0 = __fadd_rn(bh, ch);
-      const float bb = __fsub_rn(s0, bh);
-      float tt = __fadd_rn(__fsub_rn(bh, __fsub_rn(s0, bb)), __fsub_rn(ch, bb));
-      tt = __fadd_rn(tt, __fadd_rn(bl, cl));
-      rh = __fadd_rn(s0, tt);
-      rl = __fsub_rn(tt, __fsub_rn(rh, s0));
+      rh = bh;
+      rl = bl;
+      df_add_to(rh, rl, -ah, -al);
     }
     srh[row] = rh;
     srl[row] = rl;
   }
-  if (halves == 2) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int e = tid + 512 * i;
-      const int a = e >> 6, b = e & 63;
-      if (!trans) sC[a][b] = cpre[i];
-      else sC[b][a] = cpre[i];
-    }
-  }
   __syncthreads();
-  // the diagonal block, eight threads per row of a 64-row half
-  const int drow = tid >> 3, dpart = tid & 7;
-  auto solve_half = [&](int hlf) {  // x = D_hlf r_hlf into (srh, srl) of that half, in place after a barrier
-    float ph = 0.f, pl = 0.f;
+  // x_blk = inv(D) (b - off-diagonal part)
+  float2 dh2 = make_float2(0.f, 0.f), dl2 = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int c = dpart * 8 + ((k + drow) & 7);
-      const float dh = sD[(2 * hlf) * kTB + drow][c], dl = sD[(2 * hlf + 1) * kTB + drow][c];
-      const float xh = srh[kTB * hlf + c], xl = srl[kTB * hlf + c];
-      const float p = __fmul_rn(dh, xh);
-      const float pe = __fmaf_rn(dh, xh, -p);
-      const float s0 = __fadd_rn(ph, p);
-      const float bb = __fsub_rn(s0, ph);
-      float tt = __fadd_rn(__fsub_rn(ph, __fsub_rn(s0, bb)), __fsub_rn(p, bb));
-      tt = __fadd_rn(tt, __fadd_rn(pl, __fmaf_rn(dh, xl, __fmaf_rn(dl, xh, pe))));
-      ph = __fadd_rn(s0, tt);
-      pl = __fsub_rn(tt, __fsub_rn(ph, s0));
-    }
-    df_oct_sum(ph, pl);
-    __syncthreads();  // every thread has read r of this half
-    if (dpart == 0) {
-      srh[kTB * hlf + drow] = ph;
-      srl[kTB * hlf + drow] = pl;
-    }
-    __syncthreads();
-  };
-  solve_half(first);
-  if (halves == 2) {
-    // r_second -= T x_first
-    float ah2 = 0.f, al2 = 0.f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int c = dpart * 8 + ((k + drow) & 7);
-      df_fma(sC[drow][c], srh[kTB * first + c], srl[kTB * first + c], ah2, al2);
-    }
-    df_oct_sum(ah2, al2);
-    if (dpart == 0) {
-      const int i = kTB * second + drow;
-      const float ch = -ah2, cl = -al2, rh0 = srh[i], rl0 = srl[i];
-      const float s0 = __fadd_rn(rh0, ch);
-      const float bb = __fsub_rn(s0, rh0);
-      float tt = __fadd_rn(__fsub_rn(rh0, __fsub_rn(s0, bb)), __fsub_rn(ch, bb));
-      tt = __fadd_rn(tt, __fadd_rn(rl0, cl));
-      const float nh = __fadd_rn(s0, tt);
-      srh[i] = nh;
-      srl[i] = __fsub_rn(tt, __fsub_rn(nh, s0));
-    }
-    __syncthreads();
-    solve_half(second);
+  for (int k = 0; k < 16; ++k) {
+    const int c = part * 32 + 2 * ((k + 4 * part) & 15);
+    df_fma_x2(*reinterpret_cast<const float2*>(&sDh[row][c]), *reinterpret_cast<const float2*>(&sDl[row][c]),
+              *reinterpret_cast<const float2*>(&srh[c]), *reinterpret_cast<const float2*>(&srl[c]), dh2, dl2);
   }
-  if (tid < rows) {
-    const float ph = srh[tid], pl = srl[tid];
-    xh_g[r0 + tid] = ph;
-    xl_g[r0 + tid] = pl;
-    x[r0 + tid] = double(ph) + double(pl);
+  float ph = dh2.x, pl = dl2.x;
+  df_add_to(ph, pl, dh2.y, dl2.y);
+  df_quad_sum(ph, pl);
+  if (part == 0 && row < rows) {
+    xh_g[r0 + row] = ph;
+    xl_g[r0 + row] = pl;
+    x[r0 + row] = double(ph) + double(pl);
   }
   __syncthreads();
   if (tid == 0) {
@@ -1771,7 +1720,7 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
 
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
-              const float* dinv, float* xh, float* xl) {
+              const float* dinv, float* xh, float* xl, const float* dinv128) {
   const int nblk = int(ceil_div(n, kTB));
   StatScope sc(kStatTrsv, s, double(n) * n, double(n) * n * 0.5 * sizeof(TF));
   UPDES_CUDA_TRY(cudaMemsetAsync(sync_ws, 0, sizeof(int) * (nblk + 2), s));
@@ -1785,7 +1734,7 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
         const char* v = std::getenv("UPDES_TRSV_BLOCK");
         return !(v && std::atoi(v) == 64);
       }();
-      if (rows128) {
+      if (rows128 && dinv128) {
         static std::atomic<unsigned long long> attr128[4] = {};
         int e;
         if ((e = smem_opt_in((const void*)trsv128_f32_kernel<0>, int(kTrsv128Smem), attr128[0])) ||
@@ -1795,10 +1744,10 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
           return e;
         const unsigned g = unsigned(ceil_div(n, kTB2));
         switch (mode) {
-          case 0: trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
-          case 1: trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
-          case 2: trsv128_f32_kernel<2><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
-          default: trsv128_f32_kernel<3><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv); break;
+          case 0: trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
+          case 1: trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
+          case 2: trsv128_f32_kernel<2><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
+          default: trsv128_f32_kernel<3><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
         }
         UPDES_LAUNCH_CHECK();
         return UPDES_OK;
@@ -1844,9 +1793,9 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
 }
 
 template int trsv_impl<double>(int, const double*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
-                               const float*, float*, float*);
+                               const float*, float*, float*, const float*);
 template int trsv_impl<float>(int, const float*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
-                              const float*, float*, float*);
+                              const float*, float*, float*, const float*);
 
 namespace {
 
@@ -1900,6 +1849,90 @@ __global__ void __launch_bounds__(128) diag_inverse_kernel(const float* __restri
 }  // namespace
 
 size_t diag_inverse_bytes(int n) { return size_t(ceil_div(n, kTB)) * 4 * kTB * kTB * sizeof(float); }
+
+namespace {
+
+// Inverses of the 128 x 128 diagonal blocks, composed in FP64 from the two 64 x 64 inverses of
+// diag_inverse_kernel (read back from their double-float planes) and the coupling tile T of the factors:
+//   unit lower:  inv [[A, 0], [T, B]] = [[inv A, 0], [-inv B T inv A, inv B]]
+//   upper:       inv [[A, T], [0, B]] = [[inv A, -inv A T inv B], [0, inv B]]
+// blockIdx.y = 0 for L, 1 for U; out: per (block, factor) the hi and lo planes of the 128 x 128 inverse.
+__global__ void __launch_bounds__(256) diag_inverse128_kernel(const float* __restrict__ F, int64_t ldf, int n,
+                                                              const float* __restrict__ dinv64,
+                                                              float* __restrict__ dinv128) {
+  extern __shared__ double d128_smem[];
+  double(*Xa)[kTB + 1] = reinterpret_cast<double(*)[kTB + 1]>(d128_smem);
+  double(*Xb)[kTB + 1] = Xa + kTB;
+  double(*T)[kTB + 1] = Xb + kTB;
+  double(*P)[kTB + 1] = T + kTB;
+  const int blk = blockIdx.x, which = blockIdx.y, tid = threadIdx.x;
+  const int r0 = blk * 2 * kTB, rows = min(2 * kTB, n - r0);
+  const bool two = rows > kTB;
+  const int rb = rows - kTB;  // rows of the second half
+  for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+    const int i = e >> 6, j = e & 63;
+    const float* a = dinv64 + (size_t(2 * blk) * 4 + which * 2) * kTB * kTB;
+    Xa[i][j] = double(a[e]) + double(a[kTB * kTB + e]);
+    double xb = 0.0, tv = 0.0;
+    if (two) {
+      const float* b = dinv64 + (size_t(2 * blk + 1) * 4 + which * 2) * kTB * kTB;
+      xb = double(b[e]) + double(b[kTB * kTB + e]);
+      if (which == 0) {
+        if (i < rb) tv = double(F[int64_t(r0 + kTB + i) * ldf + r0 + j]);
+      } else {
+        if (j < rb) tv = double(F[int64_t(r0 + i) * ldf + r0 + kTB + j]);
+      }
+    }
+    Xb[i][j] = xb;
+    T[i][j] = tv;
+  }
+  __syncthreads();
+  if (two) {
+    // P = T inv A (lower) or T inv B (upper); then the off-diagonal block -inv B P or -inv A P into T
+    for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+      const int i = e >> 6, j = e & 63;
+      double acc = 0.0;
+      for (int k = 0; k < kTB; ++k) acc = fma(T[i][k], which == 0 ? Xa[k][j] : Xb[k][j], acc);
+      P[i][j] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+      const int i = e >> 6, j = e & 63;
+      double acc = 0.0;
+      for (int k = 0; k < kTB; ++k) acc = fma(which == 0 ? Xb[i][k] : Xa[i][k], P[k][j], acc);
+      T[i][j] = -acc;
+    }
+    __syncthreads();
+  }
+  float* hi = dinv128 + (size_t(blk) * 2 + which) * 2 * (2 * kTB) * (2 * kTB);
+  float* lo = hi + (2 * kTB) * (2 * kTB);
+  for (int e = tid; e < 4 * kTB * kTB; e += blockDim.x) {
+    const int i = e >> 7, j = e & 127;
+    const int qi = i >> 6, qj = j >> 6, ii = i & 63, jj = j & 63;
+    double v = 0.0;
+    if (qi == 0 && qj == 0) v = Xa[ii][jj];
+    else if (qi == 1 && qj == 1) v = two ? Xb[ii][jj] : 0.0;
+    else if (two && which == 0 && qi == 1 && qj == 0) v = T[ii][jj];
+    else if (two && which == 1 && qi == 0 && qj == 1) v = T[ii][jj];
+    const float h = float(v);
+    hi[e] = h;
+    lo[e] = float(v - double(h));
+  }
+}
+
+}  // namespace
+
+size_t diag_inverse128_bytes(int n) { return size_t(ceil_div(n, 2 * kTB)) * 4 * (2 * kTB) * (2 * kTB) * sizeof(float); }
+
+int diag_inverse128(int n, const float* F, int64_t ldf, const float* dinv64, float* dinv128, cudaStream_t s) {
+  const size_t smem = 4 * kTB * (kTB + 1) * sizeof(double);
+  static std::atomic<unsigned long long> attr{0};
+  if (int e = smem_opt_in((const void*)diag_inverse128_kernel, int(smem), attr)) return e;
+  StatScope sc(kStatOther, s, 4.0 * kTB * kTB * kTB * ceil_div(n, 2 * kTB), diag_inverse128_bytes(n));
+  diag_inverse128_kernel<<<dim3(unsigned(ceil_div(n, 2 * kTB)), 2), 256, smem, s>>>(F, ldf, n, dinv64, dinv128);
+  UPDES_LAUNCH_CHECK();
+  return UPDES_OK;
+}
 
 int diag_inverse(int n, const float* F, int64_t ldf, float* dinv, cudaStream_t s) {
   const size_t smem = 3 * kTB * (kTB + 1) * sizeof(double);

@@ -22,13 +22,17 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
 // instead of the substitution inside each block.
 // xh, xl (n FP32 each, may be null): scratch planes that carry solved blocks in double-float between CTAs
 // (used together with dinv).
+// dinv128 (with dinv, xh, xl): inverted 128 x 128 diagonal blocks from diag_inverse128, for the 128-row solve.
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
-              const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr);
+              const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr, const float* dinv128 = nullptr);
 
 // Inverses of the 64 x 64 diagonal blocks of FP32 LU factors, as double-float planes (diag_inverse_bytes).
 size_t diag_inverse_bytes(int n);
 int diag_inverse(int n, const float* F, int64_t ldf, float* dinv, cudaStream_t s);
+// Inverses of the 128 x 128 diagonal blocks, composed from those of diag_inverse (diag_inverse128_bytes).
+size_t diag_inverse128_bytes(int n);
+int diag_inverse128(int n, const float* F, int64_t ldf, const float* dinv64, float* dinv128, cudaStream_t s);
 
 // Mixed LU on a double-float working matrix (Whi, Wlo FP32 planes): factors in FP32 (overwriting Whi),
 // every trailing update formed exactly on the tensor cores and accumulated in double-float.

@@ -550,22 +550,23 @@ int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t l
 // x (contiguous, n) <- A^-1 x or A^-T x using the permutation in piv[n, 2n)
 template <typename TF>
 int solve_core(int n, const TF* F, int64_t ldf, const int32_t* piv, double* x, int trans, const LuWs& w,
-               cudaStream_t s, const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr) {
+               cudaStream_t s, const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr,
+               const float* dinv128 = nullptr) {
   const int32_t* perm = piv + n;
   const unsigned g = unsigned(ceil_div(n, 256));
   if (!trans) {
     permute_kernel<<<g, 256, 0, s>>>(w.tmp, x, 1, 1, perm, n, 0);
     UPDES_LAUNCH_CHECK();
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv, xh, xl);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv, xh, xl, dinv128);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv, xh, xl);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv, xh, xl, dinv128);
     if (e) return e;
     UPDES_CUDA_TRY(cudaMemcpyAsync(x, w.tmp, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
   } else {
     UPDES_CUDA_TRY(cudaMemcpyAsync(w.tmp, x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv, xh, xl);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv, xh, xl, dinv128);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv, xh, xl);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv, xh, xl, dinv128);
     if (e) return e;
     permute_kernel<<<g, 256, 0, s>>>(x, w.tmp, 1, 1, perm, n, 1);
     UPDES_LAUNCH_CHECK();
@@ -659,7 +660,8 @@ struct SolveWs {
   float *xh, *xl;    // FP32 planes of the vector a GEMV multiplies
   float* F32;  // hi plane = FP32 factors
   float* Wlo;
-  float* dinv;  // inverted 64 x 64 diagonal blocks of the FP32 factors (double-float planes)
+  float* dinv;     // inverted 64 x 64 diagonal blocks of the FP32 factors (double-float planes)
+  float* dinv128;  // the same for 128 x 128 blocks
   int32_t* piv;
   int32_t* state;  // [0] n of the factored system, [1] precision of its factors, [2] 1 when valid
   int64_t ld;
@@ -683,6 +685,7 @@ size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* ou
   w.piv = c.take<int32_t>(2 * size_t(n));
   w.state = c.take<int32_t>(64);
   w.dinv = c.take<float>(diag_inverse_bytes(n) / sizeof(float));
+  w.dinv128 = c.take<float>(diag_inverse128_bytes(n) / sizeof(float));
   w.evp = c.take<double>(eval_values_sym_bytes(n) / sizeof(double));
   w.dr = c.take<double>(n);
   w.dc = c.take<double>(n);
@@ -802,7 +805,7 @@ int residual_scaled(const SolveWs& w, int n, const double* x, double* out, doubl
 
 int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s, bool trans = false) {
   if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
-  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv, w.xh, w.xl);
+  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv, w.xh, w.xl, w.dinv128);
 }
 
 [[maybe_unused]] double host_norm(const std::vector<double>& v) {
@@ -958,6 +961,7 @@ int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info,
     UPDES_CUDA_TRY(cudaMemcpyAsync(w.Wlo, w.Klo, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
     e = factor_df_core(n, w.F32, w.Wlo, w.ld, w.piv, w.lu, s);
     if (!e) e = diag_inverse(n, w.F32, w.ld, w.dinv, s);
+    if (!e) e = diag_inverse128(n, w.F32, w.ld, w.dinv, w.dinv128, s);
   }
   if (e) return e;
   DeviceStatus h;
