@@ -17,12 +17,15 @@
 // Structure.  A pre-pass writes the digits once per update (A as [3][m][Kp] bf16, B transposed as
 // [3][nc][Kp] bf16, Kp = K rounded up to 64, zero padded) and the scales.  The main kernel is persistent
 // (one CTA per SM, tiles of 128 x 64 taken round robin) with three roles:
-//   warp 0      TMA producer: the 3 + 3 digit tiles of a k block into a 3-stage ring (128B swizzle);
+//   warp 0      TMA producer: the 3 + 3 digit tiles of a k block into a 2-stage ring (128B swizzle, 72 KB
+//               a stage, the most that fits beside the C tile);
 //   warp 1      MMA issuer: 8 products x 4 k-steps of tcgen05.mma (kind::f16, M=128, N=64) into one of
 //               two accumulator sets (4 groups x 64 columns each, 512 TMEM columns in all);
-//   warps 2-9   epilogue: tcgen05.ld of the 4 groups, fold, and at the end of a tile C -= acc.
-// The fold of one k block runs while the tensor cores work on the next, and the C read-modify-write of a
-// tile overlaps the MMAs of the following tile.  Every mbarrier wait is bounded; a timeout sets the status
+//   warps 2-17  epilogue: tcgen05.ld of the 4 groups, fold, and at the end of a tile C -= acc on the C tile
+//               in shared memory; one of its threads stores the tile by TMA and, once the store has read
+//               the buffer, loads the next tile's C into it.
+// The fold of one k block runs while the tensor cores work on the next, the C read-modify-write of a tile
+// overlaps the MMAs of the following tile, and the operand stream never waits for the C buffer.  Every mbarrier wait is bounded; a timeout sets the status
 // word and an abort flag that every role checks, and tensor memory is freed on every path.
 #include <atomic>
 
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(256) digits_cols_kernel(const float* __restric
 
 // ---- main kernel ---------------------------------------------------------------------------------------
 struct Ctrl {
-  uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], cfull, cfree, cready;
+  uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], cfull, cready;
   uint32_t tmem;
   int abort_flag;
 };
@@ -305,7 +308,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&ctl.tempty[s], kEpiWarps);
     }
     mbar_init(&ctl.cfull, 1);
-    mbar_init(&ctl.cfree, 1);
     mbar_init(&ctl.cready, kEpiWarps);
     ctl.abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -329,8 +331,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmCh)) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmCl)) : "memory");
-      int j = 0, tl = 0, last_c = -1;  // last_c: local index of the tile whose C load was issued last
-      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, ++tl) {
+      int j = 0;
+      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
         const int r0 = (t / tiles_n) * TM, c0 = (t % tiles_n) * TN;
         for (int kb = 0; kb < nkb; ++kb, ++j) {
           const int s = j % kStages;
@@ -348,20 +350,6 @@ __global__ void __launch_bounds__(kThreads, 1)
             tma_load_3d(smem_u32(sA + p * kATile), &tmA, kb * TK, r0, p, &ctl.full[s]);
             tma_load_3d(smem_u32(sB + p * kBTile), &tmB, kb * TK, c0, p, &ctl.full[s]);
           }
-          if (kb == 0) {
-            // this tile's C (hi and lo planes), once the previous tile's C has been stored from the buffer
-            if (!mbar_wait(&ctl.cfree, (uint32_t(tl) & 1u) ^ 1u, abort_flag)) {
-              if (!*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 44); }
-              *abort_flag = 1;
-              break;
-            }
-            mbar_expect_tx(&ctl.cfull, uint32_t(kCBytes));
-            tma_load_2d(smem_u32(sC), &tmCh, c0, r0, &ctl.cfull);
-            tma_load_2d(smem_u32(sC + kCHalf), &tmCh, c0 + 32, r0, &ctl.cfull);
-            tma_load_2d(smem_u32(sC + 2 * kCHalf), &tmCl, c0, r0, &ctl.cfull);
-            tma_load_2d(smem_u32(sC + 3 * kCHalf), &tmCl, c0 + 32, r0, &ctl.cfull);
-            last_c = tl;
-          }
         }
       }
       if (*abort_flag) {
@@ -369,12 +357,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int jj = (j > kStages ? j - kStages : 0); jj < j; ++jj) {
           for (long long it = 0; it < (1 << 22); ++it) {
             if (mbar_try_wait(&ctl.full[jj % kStages], uint32_t(jj / kStages) & 1u)) break;
-            __nanosleep(64);
-          }
-        }
-        if (last_c >= 0) {
-          for (long long it = 0; it < (1 << 22); ++it) {
-            if (mbar_try_wait(&ctl.cfull, uint32_t(last_c) & 1u)) break;
             __nanosleep(64);
           }
         }
@@ -418,7 +400,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int colbase = h * kEpiCols;
     const uint32_t lane_base = uint32_t(q * 32) << 16;
     int j = 0, tl = 0;
-    const bool storer = (warp == 2 && lane == 0);  // issues the C stores and frees the C buffer
+    // the storer stores each tile's C and, as soon as the store has read the buffer, loads the next tile's C
+    // into it, so that the operand stream of the producer never waits on the C buffer
+    const bool storer = (warp == 2 && lane == 0);
+    int c_pending = -1;  // storer: local index of the tile whose C load is in flight and not yet waited for
+    auto load_c = [&](int t_next, int tl_next) {
+      const int r0n = (t_next / tiles_n) * TM, c0n = (t_next % tiles_n) * TN;
+      mbar_expect_tx(&ctl.cfull, uint32_t(kCBytes));
+      tma_load_2d(smem_u32(sC), &tmCh, c0n, r0n, &ctl.cfull);
+      tma_load_2d(smem_u32(sC + kCHalf), &tmCh, c0n + 32, r0n, &ctl.cfull);
+      tma_load_2d(smem_u32(sC + 2 * kCHalf), &tmCl, c0n, r0n, &ctl.cfull);
+      tma_load_2d(smem_u32(sC + 3 * kCHalf), &tmCl, c0n + 32, r0n, &ctl.cfull);
+      c_pending = tl_next;
+    };
+    if (storer && blockIdx.x < ntiles) load_c(blockIdx.x, 0);
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
       const int r0 = (t / tiles_n) * TM, c0 = (t % tiles_n) * TN;
       const int gr = r0 + row_in_tile;
@@ -488,6 +483,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         *abort_flag = 1;
         break;
       }
+      if (storer) c_pending = -1;
       {
         // this thread's row in the 128B-swizzled boxes: 16-byte chunk q of row r sits at chunk q ^ (r & 7)
         const int r = row_in_tile;
@@ -530,11 +526,20 @@ __global__ void __launch_bounds__(kThreads, 1)
         tma_store_2d(&tmCl, c0 + 32, r0, smem_u32(sC + 3 * kCHalf));
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
         asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the buffer has been read
-        mbar_arrive(&ctl.cfree);
+        if (t + int(gridDim.x) < ntiles && !*abort_flag) load_c(t + int(gridDim.x), tl + 1);
       }
       if (__any_sync(0xffffffffu, stop)) break;  // the whole warp leaves together
     }
-    if (storer) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete before exit
+    if (storer) {
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // stores complete before exit
+      if (c_pending >= 0) {
+        // a C load still in flight (only after an abort) must land before shared memory goes away (bounded)
+        for (long long it = 0; it < (1 << 22); ++it) {
+          if (mbar_try_wait(&ctl.cfull, uint32_t(c_pending) & 1u)) break;
+          __nanosleep(64);
+        }
+      }
+    }
   }
 
   // ---- teardown: all roles done; make sure no MMA is in flight before tensor memory is freed ----
