@@ -447,22 +447,53 @@ int num_sms() {
 // FP32 panel of the mixed LU with one exchange per column and look-ahead.
 //
 // G <= 32 CTAs each hold a block of the panel's rows in shared memory.  For every column j, each CTA
-// publishes one record: its best candidate (|a|, row) together with that row's 64 values, and the owner of
-// the diagonal position publishes the row sitting there.  A reader waits for the G tags and then fetches all
-// records in one round trip, so every CTA finds the pivot and both rows of the interchange without a second
-// exchange.  The records are published right after the look-ahead step (column j+1 updated and searched),
-// before the rank-1 update of the other columns, which then overlaps the exchange; a published row therefore
-// still lacks that last update for columns >= j+2, and readers apply it with the same fused multiply-add
-// (bitwise the same values as the owner's).
+// publishes one record: its best candidate (|a|, row) together with that row's values, and the owner of the
+// diagonal position publishes the row sitting there.  Every entry of a record is an 8-byte word holding the
+// column's tag (global column + 1) in its high half and a 32-bit value in its low half, stored and loaded as
+// one single-copy-atomic access, so an entry whose tag matches is that column's value: the publisher needs
+// no fence.  The header is stored after the CTA barrier that follows the row stores; G + 1 reader threads
+// wait for the headers, then the CTA fetches every entry in one round trip and re-reads (bounded) any
+// entry whose tag is not yet the column's.  A CTA that gives up on a wait records a timeout and returns;
+// the others then give up on their own bounded waits for its records.  Every CTA finds the pivot and both rows of the
+// interchange without a second exchange.  The records are published right after the look-ahead step (column
+// j+1 updated and searched), before the rank-1 update of the other columns, which then overlaps the
+// exchange; a published row therefore still lacks that last update for columns >= j+2, and readers apply it
+// with the same fused multiply-add (bitwise the same values as the owner's).  Records alternate between two
+// slots by column parity: a CTA publishes column j+2 into column j's slot only after reading every record of
+// column j+1, which each CTA publishes only after it has read column j's.
 struct alignas(16) PanelRec {
-  unsigned int tag;  // global column + 1 this record belongs to (written last)
-  int idx;           // candidate row (INT_MAX: none)
-  float absval;
-  float pad;
-  float row[kLuNb];
+  unsigned long long idx;         // candidate row (INT_MAX: none); the diagonal record: the diagonal row
+  unsigned long long absval;      // |a| of the candidate
+  unsigned long long row[kLuNb];  // the candidate's row (the diagonal record: the row at the diagonal)
 };
+
+__device__ __forceinline__ void st_tagged(unsigned long long* p, unsigned long long tag, uint32_t bits) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(tag | bits) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_tagged(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Two adjacent tagged entries in one 16-byte load from L2 (bypassing L1, so a re-read sees new stores).
+// Each 8-byte half is validated by its own tag; these plain loads pipeline, where strong loads of one
+// thread are performed one after another.
+__device__ __forceinline__ ulonglong2 ld_tagged_pair(const unsigned long long* p) {
+  ulonglong2 v;
+  asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+  return v;
+}
+
+// Order key of a pivot candidate's |a| (-1: no candidate; NaN has been mapped to +inf): 0 for none, else
+// the float's bits + 1, which orders non-negative floats as unsigned integers.
+__device__ __forceinline__ unsigned cand_key(float v) { return v < 0.f ? 0u : __float_as_uint(v) + 1u; }
+__device__ __forceinline__ float cand_val(unsigned key) { return key ? __uint_as_float(key - 1u) : -1.f; }
 constexpr int kMaxPanelCtas = 32;
 constexpr int kPanelF32Threads = 512;  // 16 warps: the rank-1 update and the searches split over more rows
+// 16-byte entry pairs a thread fetches: G records (header pair and row pairs) and the diagonal row's pairs
+constexpr int kPanelFetch = (kMaxPanelCtas * (1 + kLuNb / 2) + kLuNb / 2 + kPanelF32Threads - 1) / kPanelF32Threads;
 
 __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, int64_t ld, int n, int k, int nb,
                                                                   int rows_per_cta, int32_t* __restrict__ piv,
@@ -476,11 +507,10 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
   float* drow = crow[kMaxPanelCtas];                                      // 64: row at the diagonal position
   float* prow = drow + kLuNb;                                             // 64: this column's pivot row
   float* pprev = prow + kLuNb;                                            // 64: the previous column's pivot row
-  __shared__ float s_cval[kMaxPanelCtas];
+  __shared__ unsigned s_ckey[kMaxPanelCtas];
   __shared__ int s_cidx[kMaxPanelCtas];
-  __shared__ float red_v[kPanelF32Threads / 32];
-  __shared__ int red_i[kPanelF32Threads / 32];
-  __shared__ int s_best;  // local candidate (tile row) for the next column, -1 if none
+  __shared__ unsigned red_k[kPanelF32Threads / 32];
+  __shared__ unsigned red_i[kPanelF32Threads / 32];
 
   const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int rbase = k + g * rows_per_cta;
@@ -491,104 +521,153 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
     for (int c = lane; c < nb; c += 32) tile[int64_t(l) * ldt + c] = W[int64_t(rbase + l) * ld + k + c];
   __syncthreads();
 
-  // local argmax of column j over this CTA's rows with global index >= from (NaN wins; smallest row on ties)
-  auto local_best = [&](int j, int from) {
-    float bv = -1.f;
-    int bi = 0x7fffffff;
-    for (int l = max(0, from - rbase) + tid; l < rcount; l += blockDim.x) {
+  // this thread's candidate for column j over its rows l (local) in [l_from, rcount), stepping by the CTA's
+  // threads: the largest |a| (NaN counts as +inf), the smallest row on ties
+  auto scan = [&](int j, int l_from, unsigned& key, unsigned& row) {
+    for (int l = l_from + tid; l < rcount; l += blockDim.x) {
       const float v = fabsf(tile[int64_t(l) * ldt + j]);
-      const float vv = (v != v) ? INFINITY : v;
-      const int gr = rbase + l;
-      if (vv > bv || (vv == bv && gr < bi)) { bv = vv; bi = gr; }
+      const unsigned kv = cand_key((v != v) ? INFINITY : v);
+      if (kv > key) { key = kv; row = unsigned(rbase + l); }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-    }
-    if (lane == 0) { red_v[wid] = bv; red_i[wid] = bi; }
-    __syncthreads();
-    if (tid < 32) {
-      bv = tid < kW ? red_v[tid] : -1.f;
-      bi = tid < kW ? red_i[tid] : 0x7fffffff;
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-      }
-      if (tid == 0) {
-        red_v[0] = bv;
-        red_i[0] = bi;
-        s_best = (bi == 0x7fffffff) ? -1 : bi - rbase;
-      }
-    }
-    __syncthreads();
   };
-
-  // publish the records of column j (candidate; the diagonal row if this CTA owns position k + j)
-  auto publish = [&](int j) {
+  // The CTA's candidate for column j from every thread's (key, row), and the records of column j: the
+  // candidate (header and row) and, by the owner of position k + j, the row there.  Warps 0 and 1 finish the
+  // argmax over the 16 warp results themselves and publish the candidate's row; warps 2 and 3 publish the
+  // diagonal row.  The barrier after the row stores keeps the published rows from being changed by the
+  // rank-1 update before they are read, and the headers, which readers wait for, are stored after it.
+  auto publish = [&](int j, unsigned key, unsigned row) {
+    unsigned km = __reduce_max_sync(0xffffffffu, key);
+    unsigned rm = __reduce_min_sync(0xffffffffu, key == km ? row : 0xffffffffu);
+    if (lane == 0) { red_k[wid] = km; red_i[wid] = rm; }
+    __syncthreads();
     const int par = j & 1, diag = k + j;
+    const unsigned long long tag = static_cast<unsigned long long>(unsigned(diag + 1)) << 32;
     PanelRec* mine = recs + par * (kMaxPanelCtas + 1) + g;
     PanelRec* drec = recs + par * (kMaxPanelCtas + 1) + kMaxPanelCtas;
-    const bool own_diag = diag >= rbase && diag < rbase + rcount;
-    if (s_best >= 0 && tid < nb) __stcg(&mine->row[tid], tile[int64_t(s_best) * ldt + tid]);
-    if (own_diag && tid >= 64 && tid < 64 + nb) __stcg(&drec->row[tid - 64], tile[int64_t(diag - rbase) * ldt + tid - 64]);
-    if (tid == 0) {
-      __stcg(&mine->idx, red_i[0]);
-      __stcg(&mine->absval, red_v[0]);
+    if (tid < 64) {
+      const unsigned k2 = lane < kW ? red_k[lane] : 0u, r2 = lane < kW ? red_i[lane] : 0x7fffffffu;
+      km = __reduce_max_sync(0xffffffffu, k2);
+      rm = __reduce_min_sync(0xffffffffu, k2 == km ? r2 : 0xffffffffu);
+      const int best = (rm == 0x7fffffffu) ? -1 : int(rm) - rbase;  // local row; -1: no candidate (zero row)
+      if (tid < nb) st_tagged(&mine->row[tid], tag, __float_as_uint(best >= 0 ? tile[int64_t(best) * ldt + tid] : 0.f));
+    } else if (tid < 128 && diag >= rbase && diag < rbase + rcount) {
+      const int c = tid - 64;
+      if (c < nb) st_tagged(&drec->row[c], tag, __float_as_uint(tile[int64_t(diag - rbase) * ldt + c]));
     }
     __syncthreads();
     if (tid == 0) {
-      __threadfence();
-      atomicExch(&mine->tag, unsigned(diag + 1));
-      if (own_diag) atomicExch(&drec->tag, unsigned(diag + 1));
+      st_tagged(&mine->absval, tag, __float_as_uint(cand_val(km)));
+      st_tagged(&mine->idx, tag, rm);
+    } else if (tid == 64 && diag >= rbase && diag < rbase + rcount) {
+      st_tagged(&drec->idx, tag, unsigned(diag));
     }
   };
 
-  local_best(0, k);
-  publish(0);
+  {
+    unsigned key = 0u, row = 0x7fffffffu;
+    scan(0, 0, key, row);
+    publish(0, key, row);
+  }
   bool prev_ok = false;  // the previous column's pivot was usable, so its update is pending in published rows
   for (int j = 0; j < nb; ++j) {
     const int par = j & 1, diag = k + j;
     const PanelRec* base = recs + par * (kMaxPanelCtas + 1);
-    // wait (bounded) for the G candidate records and the diagonal row
+    const unsigned want = unsigned(diag + 1);
+    // wait (bounded) for the headers of the G candidate records and of the diagonal record
+    bool gave_up = false;
     if (tid <= G) {
-      const PanelRec* r = (tid < G) ? base + tid : base + kMaxPanelCtas;
-      const volatile unsigned int* tw = &r->tag;
+      const unsigned long long* hp = (tid < G) ? &base[tid].idx : &base[kMaxPanelCtas].idx;
       long long it = 0;
-      while (*tw != unsigned(diag + 1)) {
+      while (unsigned(ld_tagged(hp) >> 32) != want) {
         if (++it > kSpinLimit) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 2);
+          gave_up = true;
           break;
         }
-        __nanosleep(20);
+        if (it > 64) __nanosleep(20);  // the exchange normally lands within a few round trips: poll hot first
       }
-      __threadfence();
     }
-    if (__syncthreads_or(*reinterpret_cast<volatile int*>(&st->error) != 0)) return;
-    // one round trip: every record's header and row, and the diagonal row
-    for (int e = tid; e < G * (kLuNb / 4); e += blockDim.x) {
-      const int w = e >> 4, q = e & 15;
-      reinterpret_cast<float4*>(crow[w])[q] = __ldcg(reinterpret_cast<const float4*>(base[w].row) + q);
+    if (__syncthreads_or(gave_up)) return;
+    // one round trip: each thread loads its entry pairs at once (a candidate record's header pair and row
+    // pairs, the diagonal row's pairs) and re-reads, bounded, a pair with an entry not yet this column's
+    {
+      const int half = (nb + 1) >> 1, pairs = 1 + half, total = G * pairs + half;
+      // pair e: pair e % pairs of candidate record e / pairs (0: idx and absval, then row pairs), then the
+      // diagonal record's row pairs; rc = the pair's first row entry (-1 for the header pair)
+      auto entry = [&](int e, int& rc) -> const unsigned long long* {
+        if (e >= G * pairs) {
+          rc = 2 * (e - G * pairs);
+          return &base[kMaxPanelCtas].row[rc];
+        }
+        const PanelRec* r = base + e / pairs;
+        const int c = e % pairs;
+        rc = c == 0 ? -1 : 2 * (c - 1);
+        return c == 0 ? &r->idx : &r->row[rc];
+      };
+      const unsigned long long wtag = static_cast<unsigned long long>(want) << 32;
+      // a pair is this column's once both halves carry its tag; the second entry of an odd row's last pair
+      // is not published and is not checked
+      auto fresh = [&](ulonglong2 x, int rc) {
+        return unsigned(x.x >> 32) == want && (rc + 1 >= nb || unsigned(x.y >> 32) == want);
+      };
+      ulonglong2 v[kPanelFetch];
+      int rcs[kPanelFetch];
+#pragma unroll
+      for (int u = 0; u < kPanelFetch; ++u) {
+        const int e = tid + u * kPanelF32Threads;
+        rcs[u] = -1;
+        v[u] = e < total ? ld_tagged_pair(entry(e, rcs[u])) : make_ulonglong2(wtag, wtag);
+      }
+      long long it = 0;
+      for (;;) {
+        bool pending = false;
+#pragma unroll
+        for (int u = 0; u < kPanelFetch; ++u)
+          if (!fresh(v[u], rcs[u])) {
+            pending = true;
+            v[u] = ld_tagged_pair(entry(tid + u * kPanelF32Threads, rcs[u]));
+          }
+        if (!pending) break;
+        if (++it > kSpinLimit) {
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, 3);
+          gave_up = true;
+          break;
+        }
+        if (it > 64) __nanosleep(20);
+      }
+#pragma unroll
+      for (int u = 0; u < kPanelFetch; ++u) {
+        const int e = tid + u * kPanelF32Threads;
+        if (e >= total) continue;
+        const unsigned lo = unsigned(v[u].x), hi = unsigned(v[u].y);
+        const int rc = rcs[u];
+        if (e < G * pairs) {
+          const int w = e / pairs;
+          if (rc < 0) {
+            s_cidx[w] = int(lo);
+            s_ckey[w] = cand_key(__uint_as_float(hi));
+          } else {
+            crow[w][rc] = __uint_as_float(lo);
+            if (rc + 1 < nb) crow[w][rc + 1] = __uint_as_float(hi);
+          }
+        } else {
+          drow[rc] = __uint_as_float(lo);
+          if (rc + 1 < nb) drow[rc + 1] = __uint_as_float(hi);
+        }
+      }
     }
-    if (tid < nb) drow[tid] = __ldcg(&base[kMaxPanelCtas].row[tid]);
-    if (tid < G) {
-      s_cval[tid] = __ldcg(&base[tid].absval);
-      s_cidx[tid] = __ldcg(&base[tid].idx);
+    if (__syncthreads_or(gave_up)) return;
+    // pivot: the largest |a| over the G candidates, the smallest row on ties (every warp computes it)
+    int p, gw;
+    {
+      const unsigned ck = lane < G ? s_ckey[lane] : 0u, ci = lane < G ? unsigned(s_cidx[lane]) : 0x7fffffffu;
+      const unsigned km = __reduce_max_sync(0xffffffffu, ck);
+      const unsigned im = __reduce_min_sync(0xffffffffu, ck == km ? ci : 0xffffffffu);
+      p = int(im);
+      gw = __ffs(__ballot_sync(0xffffffffu, ck == km && ci == im)) - 1;
     }
-    __syncthreads();
-    // pivot: best over the G candidates (every warp computes it; no extra barrier)
-    float bv = lane < G ? s_cval[lane] : -1.f;
-    int bi = lane < G ? s_cidx[lane] : 0x7fffffff;
-    int bw = lane;
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      const int ow = __shfl_xor_sync(0xffffffffu, bw, o);
-      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; bw = ow; }
-    }
-    const int p = bi, gw = bw;
     // the published rows still lack the previous column's update for columns >= j + 1
     if (tid < nb) {
       float pr = crow[gw][tid], dr = drow[tid];
@@ -611,19 +690,25 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
     __syncthreads();
     const int l0 = max(0, diag + 1 - rbase);
     const bool ok = (pv != 0.f && isfinite(pv));
+    // scale column j, update the look-ahead column j + 1 and take this thread's candidate for it on the way
+    unsigned key = 0u, crow_i = 0x7fffffffu;
     if (ok) {
       const float rinv = 1.0f / pv;
       for (int l = l0 + tid; l < rcount; l += blockDim.x) {
         float* row = tile + int64_t(l) * ldt;
         row[j] *= rinv;
-        if (j + 1 < nb) row[j + 1] = __fmaf_rn(-row[j], prow[j + 1], row[j + 1]);  // look-ahead column
+        if (j + 1 < nb) {
+          const float x = __fmaf_rn(-row[j], prow[j + 1], row[j + 1]);  // look-ahead column
+          row[j + 1] = x;
+          const float ax = fabsf(x);
+          const unsigned kv = cand_key((ax != ax) ? INFINITY : ax);
+          if (kv > key) { key = kv; crow_i = unsigned(rbase + l); }
+        }
       }
+    } else if (j + 1 < nb) {
+      scan(j + 1, l0, key, crow_i);
     }
-    if (j + 1 < nb) {
-      __syncthreads();
-      local_best(j + 1, diag + 1);
-      publish(j + 1);
-    }
+    if (j + 1 < nb) publish(j + 1, key, crow_i);
     // rank-1 update of the remaining columns, overlapping the exchange of the next column
     if (ok && j + 2 < nb) {
       // warp w takes rows l0 + w + 8i, four at a time for independent shared-memory traffic; lanes span columns
