@@ -451,16 +451,18 @@ int num_sms() {
 // diagonal position publishes the row sitting there.  Every entry of a record is an 8-byte word holding the
 // column's tag (global column + 1) in its high half and a 32-bit value in its low half, stored and loaded as
 // one single-copy-atomic access, so an entry whose tag matches is that column's value: the publisher needs
-// no fence.  The header is stored after the CTA barrier that follows the row stores; G + 1 reader threads
-// wait for the headers, then the CTA fetches every entry in one round trip and re-reads (bounded) any
-// entry whose tag is not yet the column's.  A CTA that gives up on a wait records a timeout and returns;
-// the others then give up on their own bounded waits for its records.  Every CTA finds the pivot and both rows of the
-// interchange without a second exchange.  The records are published right after the look-ahead step (column
-// j+1 updated and searched), before the rank-1 update of the other columns, which then overlaps the
-// exchange; a published row therefore still lacks that last update for columns >= j+2, and readers apply it
-// with the same fused multiply-add (bitwise the same values as the owner's).  Records alternate between two
-// slots by column parity: a CTA publishes column j+2 into column j's slot only after reading every record of
-// column j+1, which each CTA publishes only after it has read column j's.
+// no fence.  A record's header (the (idx, |a|) pair) is stored after the CTA barrier that follows its row
+// stores.  G + 1 reader threads wait for the headers, from which every warp finds the pivot; the CTA then
+// fetches only the pivot's row and the diagonal row, re-reading (bounded) an entry whose tag is not yet the
+// column's.  A CTA that gives up on a wait records a timeout and returns; the others then give up on their
+// own bounded waits for its records.
+//
+// The records are published right after the look-ahead step (column j+1 updated and searched), before the
+// rank-1 update of the other columns, which then overlaps the exchange; a published row therefore still
+// lacks that last update for columns >= j+2, and readers apply it with the same fused multiply-add (bitwise
+// the same values as the owner's).  Records alternate between two slots by column parity: a CTA publishes
+// column j+2 into column j's slot only after it has seen every header of column j+1, which each CTA
+// publishes only after its reads of column j's slot have returned.
 struct alignas(16) PanelRec {
   unsigned long long idx;         // candidate row (INT_MAX: none); the diagonal record: the diagonal row
   unsigned long long absval;      // |a| of the candidate
@@ -471,15 +473,14 @@ __device__ __forceinline__ void st_tagged(unsigned long long* p, unsigned long l
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(tag | bits) : "memory");
 }
 
-__device__ __forceinline__ unsigned long long ld_tagged(const unsigned long long* p) {
+// Tagged entries loaded from L2 (bypassing L1, so a re-read sees new stores): one entry, or two adjacent
+// ones in a 16-byte load, each 8-byte half validated by its own tag.
+__device__ __forceinline__ unsigned long long ld_tagged_cg(const unsigned long long* p) {
   unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 
-// Two adjacent tagged entries in one 16-byte load from L2 (bypassing L1, so a re-read sees new stores).
-// Each 8-byte half is validated by its own tag; these plain loads pipeline, where strong loads of one
-// thread are performed one after another.
 __device__ __forceinline__ ulonglong2 ld_tagged_pair(const unsigned long long* p) {
   ulonglong2 v;
   asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
@@ -492,15 +493,14 @@ __device__ __forceinline__ unsigned cand_key(float v) { return v < 0.f ? 0u : __
 __device__ __forceinline__ float cand_val(unsigned key) { return key ? __uint_as_float(key - 1u) : -1.f; }
 constexpr int kMaxPanelCtas = 32;
 constexpr int kPanelF32Threads = 512;  // 16 warps: the rank-1 update and the searches split over more rows
-// 16-byte entry pairs a thread fetches: G records (header pair and row pairs) and the diagonal row's pairs
-constexpr int kPanelFetch = (kMaxPanelCtas * (1 + kLuNb / 2) + kLuNb / 2 + kPanelF32Threads - 1) / kPanelF32Threads;
 
 __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, int64_t ld, int n, int k, int nb,
                                                                   int rows_per_cta, int32_t* __restrict__ piv,
                                                                   PanelRec* recs, int32_t* swap_map,
                                                                   DeviceStatus* st) {
   extern __shared__ __align__(16) unsigned char pf_smem[];
-  float(*crow)[kLuNb] = reinterpret_cast<float(*)[kLuNb]>(pf_smem);      // 32 x 64: the G records' rows
+  float(*crow)[kLuNb] = reinterpret_cast<float(*)[kLuNb]>(pf_smem);      // 32 x 64 (row 0: the pivot's row)
+  float* wrow = crow[0];  // the pivot's row as its record holds it
   // rows_per_cta x nb with row stride nb + 1: consecutive rows of one column fall in different banks
   float* tile = reinterpret_cast<float*>(pf_smem) + (kMaxPanelCtas + 3) * kLuNb;
   const int ldt = nb + 1;
@@ -573,12 +573,13 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
     const int par = j & 1, diag = k + j;
     const PanelRec* base = recs + par * (kMaxPanelCtas + 1);
     const unsigned want = unsigned(diag + 1);
-    // wait (bounded) for the headers of the G candidate records and of the diagonal record
+    // wait (bounded) for the headers: each candidate record's (idx, |a|) pair, the diagonal record's idx
     bool gave_up = false;
     if (tid <= G) {
       const unsigned long long* hp = (tid < G) ? &base[tid].idx : &base[kMaxPanelCtas].idx;
+      ulonglong2 h = ld_tagged_pair(hp);
       long long it = 0;
-      while (unsigned(ld_tagged(hp) >> 32) != want) {
+      while (unsigned(h.x >> 32) != want || (tid < G && unsigned(h.y >> 32) != want)) {
         if (++it > kSpinLimit) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 2);
@@ -586,76 +587,11 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
           break;
         }
         if (it > 64) __nanosleep(20);  // the exchange normally lands within a few round trips: poll hot first
+        h = ld_tagged_pair(hp);
       }
-    }
-    if (__syncthreads_or(gave_up)) return;
-    // one round trip: each thread loads its entry pairs at once (a candidate record's header pair and row
-    // pairs, the diagonal row's pairs) and re-reads, bounded, a pair with an entry not yet this column's
-    {
-      const int half = (nb + 1) >> 1, pairs = 1 + half, total = G * pairs + half;
-      // pair e: pair e % pairs of candidate record e / pairs (0: idx and absval, then row pairs), then the
-      // diagonal record's row pairs; rc = the pair's first row entry (-1 for the header pair)
-      auto entry = [&](int e, int& rc) -> const unsigned long long* {
-        if (e >= G * pairs) {
-          rc = 2 * (e - G * pairs);
-          return &base[kMaxPanelCtas].row[rc];
-        }
-        const PanelRec* r = base + e / pairs;
-        const int c = e % pairs;
-        rc = c == 0 ? -1 : 2 * (c - 1);
-        return c == 0 ? &r->idx : &r->row[rc];
-      };
-      const unsigned long long wtag = static_cast<unsigned long long>(want) << 32;
-      // a pair is this column's once both halves carry its tag; the second entry of an odd row's last pair
-      // is not published and is not checked
-      auto fresh = [&](ulonglong2 x, int rc) {
-        return unsigned(x.x >> 32) == want && (rc + 1 >= nb || unsigned(x.y >> 32) == want);
-      };
-      ulonglong2 v[kPanelFetch];
-      int rcs[kPanelFetch];
-#pragma unroll
-      for (int u = 0; u < kPanelFetch; ++u) {
-        const int e = tid + u * kPanelF32Threads;
-        rcs[u] = -1;
-        v[u] = e < total ? ld_tagged_pair(entry(e, rcs[u])) : make_ulonglong2(wtag, wtag);
-      }
-      long long it = 0;
-      for (;;) {
-        bool pending = false;
-#pragma unroll
-        for (int u = 0; u < kPanelFetch; ++u)
-          if (!fresh(v[u], rcs[u])) {
-            pending = true;
-            v[u] = ld_tagged_pair(entry(tid + u * kPanelF32Threads, rcs[u]));
-          }
-        if (!pending) break;
-        if (++it > kSpinLimit) {
-          status_error(st, UPDES_ERR_TIMEOUT);
-          atomicCAS(&st->timeout_tag, 0, 3);
-          gave_up = true;
-          break;
-        }
-        if (it > 64) __nanosleep(20);
-      }
-#pragma unroll
-      for (int u = 0; u < kPanelFetch; ++u) {
-        const int e = tid + u * kPanelF32Threads;
-        if (e >= total) continue;
-        const unsigned lo = unsigned(v[u].x), hi = unsigned(v[u].y);
-        const int rc = rcs[u];
-        if (e < G * pairs) {
-          const int w = e / pairs;
-          if (rc < 0) {
-            s_cidx[w] = int(lo);
-            s_ckey[w] = cand_key(__uint_as_float(hi));
-          } else {
-            crow[w][rc] = __uint_as_float(lo);
-            if (rc + 1 < nb) crow[w][rc + 1] = __uint_as_float(hi);
-          }
-        } else {
-          drow[rc] = __uint_as_float(lo);
-          if (rc + 1 < nb) drow[rc + 1] = __uint_as_float(hi);
-        }
+      if (tid < G) {
+        s_cidx[tid] = int(unsigned(h.x));
+        s_ckey[tid] = cand_key(__uint_as_float(unsigned(h.y)));
       }
     }
     if (__syncthreads_or(gave_up)) return;
@@ -668,11 +604,31 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
       p = int(im);
       gw = __ffs(__ballot_sync(0xffffffffu, ck == km && ci == im)) - 1;
     }
+    // the pivot's row from record gw (threads 0-63) and the diagonal row (threads 64-127), each entry
+    // re-read (bounded) until it carries the column's tag
+    if (tid < 128 && (tid & 63) < nb) {
+      const int c = tid & 63;
+      const unsigned long long* q = tid < 64 ? &base[gw].row[c] : &base[kMaxPanelCtas].row[c];
+      unsigned long long x = ld_tagged_cg(q);
+      long long it = 0;
+      while (unsigned(x >> 32) != want) {
+        if (++it > kSpinLimit) {
+          status_error(st, UPDES_ERR_TIMEOUT);
+          atomicCAS(&st->timeout_tag, 0, 3);
+          gave_up = true;
+          break;
+        }
+        if (it > 64) __nanosleep(20);
+        x = ld_tagged_cg(q);
+      }
+      (tid < 64 ? wrow : drow)[c] = __uint_as_float(unsigned(x));
+    }
+    if (__syncthreads_or(gave_up)) return;
     // the published rows still lack the previous column's update for columns >= j + 1
     if (tid < nb) {
-      float pr = crow[gw][tid], dr = drow[tid];
+      float pr = wrow[tid], dr = drow[tid];
       if (prev_ok && tid > j) {
-        pr = __fmaf_rn(-crow[gw][j - 1], pprev[tid], pr);
+        pr = __fmaf_rn(-wrow[j - 1], pprev[tid], pr);
         dr = __fmaf_rn(-drow[j - 1], pprev[tid], dr);
       }
       prow[tid] = pr;
