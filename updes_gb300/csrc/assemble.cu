@@ -552,10 +552,9 @@ struct __align__(16) DfRow {
   float c[12];              // A0..A5 as double-float pairs
 };
 
-__global__ void assemble_df_setup_kernel(updes_problem p, DfRow* __restrict__ rows, float* __restrict__ tri) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= p.N) return;
-  for (int d = 0; d < 2; ++d) {  // exact triple-float expansion of each coordinate
+// Node j's coordinates as exact triple-float expansions: tri[6j + 3d + t], d = x or y, t = 0..2.
+__device__ __forceinline__ void tri_expand(const updes_problem& p, int j, float* __restrict__ tri) {
+  for (int d = 0; d < 2; ++d) {
     const double x = p.nodes[2ll * j + d];
     const float x0 = __double2float_rn(x);
     const double r1 = x - double(x0);
@@ -564,6 +563,17 @@ __global__ void assemble_df_setup_kernel(updes_problem p, DfRow* __restrict__ ro
     tri[6ll * j + 3 * d + 1] = x1;
     tri[6ll * j + 3 * d + 2] = __double2float_rn(r1 - double(x1));
   }
+}
+
+__global__ void tri_coords_kernel(updes_problem p, float* __restrict__ tri) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < p.N) tri_expand(p, j, tri);
+}
+
+__global__ void assemble_df_setup_kernel(updes_problem p, DfRow* __restrict__ rows, float* __restrict__ tri) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= p.N) return;
+  tri_expand(p, j, tri);
   const RowInfo ri = load_row(p, j);
   const double k = 2.0 * p.rbf_param + 1.0;
   double A[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -772,15 +782,106 @@ extern "C" int updes_assemble_df(const updes_problem* p, float* Khi, float* Klo,
   return UPDES_OK;
 }
 
-size_t eval_values_sym_bytes(int N) { return size_t(ceil_div(N, kSymT)) * size_t(N) * sizeof(double); }
+// eval_values_sym_kernel for polyharmonic kernels (phi = r^(2a+1)) in double-float arithmetic on the FP32
+// pipes, for the mixed-precision solve: x_i - x_j exactly from the triple-float coordinates and rounded
+// once to double-float, phi = r (r^2)^a, the products with the coefficients (rounded to double-float) and
+// the 16-term partial sums of a thread in double-float (relative error a few units of 2^-48), the tile's
+// row and column sums in FP64 as in the FP64 kernel.  r = 0 gives phi = 0, as phi(0) = 0.
+__global__ void __launch_bounds__(256) eval_values_sym_df_kernel(updes_problem p, const double* __restrict__ coeffs,
+                                                                 const float* __restrict__ tri,
+                                                                 double* __restrict__ part) {
+  const int J = blockIdx.x, I = blockIdx.y;
+  if (I > J) return;
+  __shared__ double scol[16][kSymT + 1];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int N = p.N;
+  const int apow = int(p.rbf_param);
+  const int i0 = I * kSymT + ty * 4, j0 = J * kSymT + tx * 4;
+  float xi[4][3], yi[4][3], xj[4][3], yj[4][3];
+  F2 ci[4], cj[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = min(i0 + u, N - 1), j = min(j0 + u, N - 1);
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      xi[u][t] = tri[6ll * i + t];
+      yi[u][t] = tri[6ll * i + 3 + t];
+      xj[u][t] = tri[6ll * j + t];
+      yj[u][t] = tri[6ll * j + 3 + t];
+    }
+    ci[u] = df_from_double(i0 + u < N ? coeffs[i] : 0.0);  // padding rows and columns carry c = 0
+    cj[u] = df_from_double(j0 + u < N ? coeffs[j] : 0.0);
+  }
+  F2 racc[4], cacc[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) racc[u] = cacc[u] = F2{0.f, 0.f};
+  const bool diag = (I == J);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (diag && i0 + u == j0 + v && !p.self_term) continue;
+      const F2 dx = diff3(xi[u][0], xi[u][1], xi[u][2], xj[v][0], xj[v][1], xj[v][2]);
+      const F2 dy = diff3(yi[u][0], yi[u][1], yi[u][2], yj[v][0], yj[v][1], yj[v][2]);
+      if (dx.h == 0.f && dy.h == 0.f) continue;
+      const F2 r2 = df_add(df_sqr(dx), df_sqr(dy));
+      F2 phi = df_sqrt(r2);
+      for (int t = 0; t < apow; ++t) phi = df_mul(phi, r2);
+      racc[u] = df_add(racc[u], df_mul(phi, cj[v]));
+      cacc[v] = df_add(cacc[v], df_mul(phi, ci[u]));
+    }
+  }
+  double rs[4], cs[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    rs[u] = double(racc[u].h) + double(racc[u].l);
+    cs[u] = double(cacc[u].h) + double(cacc[u].l);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    for (int o = 8; o > 0; o >>= 1) rs[u] += __shfl_xor_sync(0xffffffffu, rs[u], o);
+  if (tx == 0)
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + u < N) part[int64_t(J) * N + i0 + u] = rs[u];
+  if (!diag) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) scol[ty][tx * 4 + v] = cs[v];
+    __syncthreads();
+    if (tid < kSymT) {
+      double sum = 0.0;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) sum += scol[q][tid];
+      const int j = J * kSymT + tid;
+      if (j < N) part[int64_t(I) * N + j] = sum;
+    }
+  }
+}
 
-// updes_eval_values through the symmetric kernel, with a scratch of eval_values_sym_bytes(N) bytes.
-int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, double* part, cudaStream_t s) {
+size_t eval_values_sym_bytes(int N) {
+  // per-tile partial sums, then the triple-float coordinates of the double-float kernel
+  return size_t(ceil_div(N, kSymT)) * size_t(N) * sizeof(double) + ((size_t(N) * 6 * sizeof(float) + 255) & ~size_t(255));
+}
+
+// updes_eval_values through the symmetric kernel, with a scratch of eval_values_sym_bytes(N) bytes; df
+// selects the double-float kernel for polyharmonic systems (the other kernels stay in FP64).
+int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, double* part, cudaStream_t s,
+                    bool df) {
   int st = check_problem(p);
   if (st) return st;
   if (!coeffs || !vals || !part) return UPDES_ERR_INVALID;
   const int nblk = int(ceil_div(p->N, kSymT));
   const dim3 grid{unsigned(nblk), unsigned(nblk)};
+  if (df && p->rbf == UPDES_RBF_POLYHARMONIC) {
+    float* tri = reinterpret_cast<float*>(part + size_t(nblk) * size_t(p->N));
+    tri_coords_kernel<<<unsigned(ceil_div(p->N, 256)), 256, 0, s>>>(*p, tri);
+    UPDES_LAUNCH_CHECK();
+    eval_values_sym_df_kernel<<<grid, 256, 0, s>>>(*p, coeffs, tri, part);
+    UPDES_LAUNCH_CHECK();
+    eval_values_sym_reduce<<<unsigned(ceil_div(p->N, 256)), 256, 0, s>>>(*p, part, nblk, coeffs, vals);
+    UPDES_LAUNCH_CHECK();
+    return UPDES_OK;
+  }
   switch (p->rbf) {
     case UPDES_RBF_POLYHARMONIC: eval_values_sym_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, coeffs, part); break;
     case UPDES_RBF_GAUSSIAN: eval_values_sym_kernel<UPDES_RBF_GAUSSIAN><<<grid, 256, 0, s>>>(*p, coeffs, part); break;

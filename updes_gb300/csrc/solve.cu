@@ -20,7 +20,8 @@
 
 int updes_check_problem(const updes_problem* p);
 size_t eval_values_sym_bytes(int N);
-int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, double* part, cudaStream_t s);
+int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, double* part, cudaStream_t s,
+                    bool df);
 
 namespace {
 
@@ -1093,16 +1094,22 @@ int solve_stage(const updes_problem* p, const SolveWs& w, int n, const double* q
     if ((e = factor_stage(w, n, precision, info, s))) return e;
   }
   Timer t(s);
+  // the values of a mixed-precision solve in double-float (polyharmonic kernels; UPDES_DF_EVAL=0: FP64)
+  static const bool df_eval_on = [] {
+    const char* v = std::getenv("UPDES_DF_EVAL");
+    return !(v && v[0] == '0');
+  }();
+  const bool df_eval = df_eval_on && precision == UPDES_PREC_FP32;
   axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.x, 0.0, n, w.dc);  // coeffs = dc .* x
   UPDES_LAUNCH_CHECK();
   if (cstride == 1) {
     UPDES_CUDA_TRY(cudaMemcpyAsync(coeffs, w.x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    if (vals && vstride == 1 && (e = eval_values_sym(p, coeffs, vals, w.evp, s))) return e;
+    if (vals && vstride == 1 && (e = eval_values_sym(p, coeffs, vals, w.evp, s, df_eval))) return e;
   } else {
     UPDES_CUDA_TRY(cudaMemcpy2DAsync(coeffs, cstride * 8, w.x, 8, 8, n, cudaMemcpyDeviceToDevice, s));
   }
   if (vals && (cstride != 1 || vstride != 1)) {
-    if ((e = eval_values_sym(p, w.x, w.wv, w.evp, s))) return e;
+    if ((e = eval_values_sym(p, w.x, w.wv, w.evp, s, df_eval))) return e;
     UPDES_CUDA_TRY(cudaMemcpy2DAsync(vals, vstride * 8, w.wv, 8, 8, p->N, cudaMemcpyDeviceToDevice, s));
   }
   info->t_eval_ms += t.stop();
