@@ -251,6 +251,30 @@ __global__ void __launch_bounds__(256) swap_rows_kernel(SwapJobs jobs, int64_t l
     if (ok) plane[int64_t(map[1 + q]) * ld + c] = buf[q][col];
 }
 
+// The interchanges of nmaps consecutive panels (swap maps kSwapMapStride ints apart) in one launch: each CTA
+// applies the maps to its columns in panel order, the order in which separate launches would apply them.
+constexpr int kSwapMapStride = 512;
+__global__ void __launch_bounds__(256) swap_rows_maps_kernel(SwapJobs jobs, int64_t ld, const int32_t* __restrict__ maps,
+                                                             int nmaps) {
+  __shared__ float buf[128][64];
+  const int j = blockIdx.y;
+  if (j >= jobs.njobs) return;
+  const int col = threadIdx.x & 63, r0 = threadIdx.x >> 6;
+  const int64_t c = jobs.c0[j] + int64_t(blockIdx.x) * 64 + col;
+  const bool ok = c < jobs.c1[j];
+  float* plane = jobs.plane[j];
+  for (int m = 0; m < nmaps; ++m) {
+    const int32_t* map = maps + m * kSwapMapStride;
+    const int cnt = map[0];
+    for (int q = r0; q < cnt; q += 4)
+      if (ok) buf[q][col] = plane[int64_t(map[129 + q]) * ld + c];
+    __syncthreads();
+    for (int q = r0; q < cnt; q += 4)
+      if (ok) plane[int64_t(map[1 + q]) * ld + c] = buf[q][col];
+    __syncthreads();  // this map's rows are in place (and buf free) before the next map reads them
+  }
+}
+
 // U = L^-1 W on rows [k, k+nb), columns [c0, c1): L unit lower from F (FP32), W double-float.  Each row is
 // w_i - sum_j L_ij x_j accumulated in double-float (exact FP32 products, compensated sums) and rounded once
 // to FP32 into F: FP32 ALU only.
@@ -800,7 +824,7 @@ int launch_panel(void* W, const float* Wlo, int64_t ldw, TF* F, int64_t ldf, int
 }
 
 constexpr int kOuterNb = 4 * kLuNb;   // 256: width of the big exact trailing updates
-constexpr int kSwapMapInts = 512;     // one panel's swap map (257 ints used): 2 KB per slot
+constexpr int kSwapMapInts = kSwapMapStride;  // one panel's swap map (257 ints used): 2 KB per slot
 constexpr int kLookaheadMinN = 1024;  // smaller factorisations run their steps in order on one stream
 constexpr int kLookaheadCtas = kMaxPanelCtas;  // SMs kept for the look-ahead block beside the trailing update
 // Below this many trailing rows the next block's factorisation (linear in the rows) outlasts the trailing
@@ -976,15 +1000,18 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   };
   // The deferred interchanges of block [K0, KE), panel by panel, on trailing columns [c0, c1) (both planes)
   // and, with left, on the factored columns [0, K0) (the FP32 factors).
+  // All the block's panels in one launch: each column chunk applies their maps in panel order.
   auto swaps_deferred = [&](int K0, int KE, int c0, int c1, bool left) -> int {
-    for (int k = K0, p = 0; k < KE; k += nb, ++p) {
-      SwapJobs j{};
-      int64_t maxc = 0;
-      if (left) add_swap_job(j, maxc, Whi, 0, K0);
-      add_swap_job(j, maxc, Whi, c0, c1);
-      add_swap_job(j, maxc, Wlo, c0, c1);
-      if (int e = swap_launch(j, maxc, swap_maps + p * kSwapMapInts, s)) return e;
-    }
+    SwapJobs j{};
+    int64_t maxc = 0;
+    if (left) add_swap_job(j, maxc, Whi, 0, K0);
+    add_swap_job(j, maxc, Whi, c0, c1);
+    add_swap_job(j, maxc, Wlo, c0, c1);
+    if (!j.njobs) return UPDES_OK;
+    const int nmaps = int(ceil_div(KE - K0, nb));
+    StatScope sc(kStatOther, s, 0.0, 2.0 * 2 * nb * maxc * 4.0 * j.njobs * nmaps);
+    swap_rows_maps_kernel<<<dim3(unsigned(ceil_div(maxc, 64)), j.njobs), 256, 0, s>>>(j, ld, swap_maps, nmaps);
+    UPDES_LAUNCH_CHECK();
     return UPDES_OK;
   };
   // Block row of U for block [K0, KE) on trailing columns [c0, c1), the updates on at most ctas CTAs.
