@@ -132,10 +132,12 @@ __global__ void col_max_f32_kernel(const float* __restrict__ Khi, int64_t ld, in
   if (m > 0.0) atomicMax(colmax + j, (unsigned long long)__double_as_longlong(m));
 }
 
-// Both planes times dr_i dc_j in place (powers of two: exact), four columns a thread, rows strided over grid.y.
+// Both planes times dr_i dc_j in place (powers of two: exact), four columns a thread, rows strided over grid.y;
+// with hi2/lo2 the scaled planes are also written there (the factorisation's working copy, in the same pass).
 __global__ void __launch_bounds__(256) scale_planes_kernel(float* __restrict__ hi, float* __restrict__ lo, int64_t ld,
                                                            int n, const double* __restrict__ dr,
-                                                           const double* __restrict__ dc) {
+                                                           const double* __restrict__ dc, float* __restrict__ hi2,
+                                                           float* __restrict__ lo2) {
   const int64_t j0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
   if (j0 >= n) return;
   float cs[4];
@@ -150,6 +152,10 @@ __global__ void __launch_bounds__(256) scale_planes_kernel(float* __restrict__ h
     l.x = l.x * rs * cs[0]; l.y = l.y * rs * cs[1]; l.z = l.z * rs * cs[2]; l.w = l.w * rs * cs[3];
     *ph = h;
     *pl = l;
+    if (hi2) {
+      *reinterpret_cast<float4*>(hi2 + int64_t(i) * ld + j0) = h;
+      *reinterpret_cast<float4*>(lo2 + int64_t(i) * ld + j0) = l;
+    }
   }
 }
 
@@ -948,7 +954,9 @@ extern "C" int updes_solve_workspace(const updes_problem* p, const updes_solve_o
 namespace {
 
 // Factors of the equilibrated K (double-float planes) at `precision`; records the factored state.
-int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info, cudaStream_t s) {
+// planes_ready: the working planes (F32, Wlo) already hold the equilibrated K (written by the assembly).
+int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info, cudaStream_t s,
+                 bool planes_ready = false) {
   Timer t(s);
   int e;
   UPDES_CUDA_TRY(cudaMemsetAsync(w.state, 0, 4 * sizeof(int32_t), s));  // invalid until the factors are complete
@@ -958,8 +966,10 @@ int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info,
     UPDES_LAUNCH_CHECK();
     e = factor_core(n, w.W, w.ld, precision, nullptr, w.ld, w.piv, w.lu, s);
   } else {
-    UPDES_CUDA_TRY(cudaMemcpyAsync(w.F32, w.Khi, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
-    UPDES_CUDA_TRY(cudaMemcpyAsync(w.Wlo, w.Klo, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
+    if (!planes_ready) {
+      UPDES_CUDA_TRY(cudaMemcpyAsync(w.F32, w.Khi, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
+      UPDES_CUDA_TRY(cudaMemcpyAsync(w.Wlo, w.Klo, size_t(total) * 4, cudaMemcpyDeviceToDevice, s));
+    }
     e = factor_df_core(n, w.F32, w.Wlo, w.ld, w.piv, w.lu, s);
     if (!e) e = diag_inverse(n, w.F32, w.ld, w.dinv, s);
     if (!e) e = diag_inverse128(n, w.F32, w.ld, w.dinv, w.dinv128, s);
@@ -1009,9 +1019,10 @@ int assemble_df_stage(const updes_problem* p, const SolveWs& w, int n, cudaStrea
   col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(n, w.dc);
   UPDES_LAUNCH_CHECK();
   {
-    StatScope sc(kStatOther, s, 0.0, double(n) * n * 16.0);
+    StatScope sc(kStatOther, s, 0.0, double(n) * n * 24.0);
+    // the factorisation's working copy (F32, Wlo) in the same pass: the assembly's scratch there is done with
     scale_planes_kernel<<<dim3(unsigned(ceil_div(n, 1024)), unsigned(std::min(n, 4096))), 256, 0, s>>>(
-        w.Khi, w.Klo, w.ld, n, w.dr, w.dc);
+        w.Khi, w.Klo, w.ld, n, w.dr, w.dc, w.F32, w.Wlo);
     UPDES_LAUNCH_CHECK();
   }
   int32_t hflag = 0;
@@ -1022,10 +1033,12 @@ int assemble_df_stage(const updes_problem* p, const SolveWs& w, int n, cudaStrea
 
 // Assemble K and its power-of-two equilibration into the double-float planes: in double-float arithmetic for
 // a polyharmonic system factored in FP32, else in FP64.
+// *planes_ready: the factorisation's working planes hold the equilibrated K as well (double-float assembly).
 int assemble_stage(const updes_problem* p, const SolveWs& w, int n, int precision, updes_solve_info* info,
-                   cudaStream_t s) {
+                   cudaStream_t s, bool* planes_ready) {
   Timer t(s);
   int e;
+  *planes_ready = false;
   // UPDES_DF_ASSEMBLY=0 assembles every system in FP64
   static const bool df_assembly = [] {
     const char* v = std::getenv("UPDES_DF_ASSEMBLY");
@@ -1035,6 +1048,7 @@ int assemble_stage(const updes_problem* p, const SolveWs& w, int n, int precisio
     e = assemble_df_stage(p, w, n, s);
     if (e != UPDES_ERR_UNSUPPORTED) {
       if (e) return e;
+      *planes_ready = true;
       info->t_assemble_ms += t.stop();
       return UPDES_OK;
     }
@@ -1142,8 +1156,9 @@ extern "C" int updes_factor(const updes_problem* p, const updes_solve_opts* opts
   std::memset(info, 0, sizeof *info);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n = p->N + p->M;
-  if ((e = assemble_stage(p, w, n, o.precision, info, s))) return e;
-  if ((e = factor_stage(w, n, o.precision, info, s))) return e;
+  bool planes_ready = false;
+  if ((e = assemble_stage(p, w, n, o.precision, info, s, &planes_ready))) return e;
+  if ((e = factor_stage(w, n, o.precision, info, s, planes_ready))) return e;
   return info->lu_info ? UPDES_ERR_SINGULAR : UPDES_OK;
 }
 
@@ -1194,8 +1209,9 @@ extern "C" int updes_solve(const updes_problem* p, const double* q, double* coef
   std::memset(info, 0, sizeof *info);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int n = p->N + p->M;
-  if ((e = assemble_stage(p, w, n, o.precision, info, s))) return e;
-  if ((e = factor_stage(w, n, o.precision, info, s))) return e;
+  bool planes_ready = false;
+  if ((e = assemble_stage(p, w, n, o.precision, info, s, &planes_ready))) return e;
+  if ((e = factor_stage(w, n, o.precision, info, s, planes_ready))) return e;
   if ((e = solve_stage(p, w, n, q, 1, coeffs, 1, vals, 1, o, info, s))) return e;
   if (info->lu_info) return UPDES_ERR_SINGULAR;
   if (!info->converged) return UPDES_ERR_NOT_CONVERGED;
