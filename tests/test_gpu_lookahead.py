@@ -42,9 +42,13 @@ for n in {sizes!r}:
 SIZES = [1024, 1300, 2113, 12600]  # 12600: the first steps fork after the whole block row, the later ones early
 
 
-def _digests(lookahead):
+def _digests(lookahead, blocking=False):
     env = dict(os.environ)
     env["UPDES_LOOKAHEAD"] = "1" if lookahead else "0"
+    if blocking:
+        # every launch completes before the next is issued: the two streams' kernels run in issue order, so a
+        # look-ahead kernel that touches data the other stream still needs shows up deterministically
+        env["CUDA_LAUNCH_BLOCKING"] = "1"
     out = subprocess.run([sys.executable, "-c", _SCRIPT.format(root=ROOT, sizes=SIZES)], env=env, check=True,
                          capture_output=True, text=True, timeout=600).stdout
     return [line.split() for line in out.strip().splitlines()]
@@ -56,6 +60,15 @@ def test_lookahead_factors_bitwise_serial():
     for (n1, i1, h1), (n2, i2, h2) in zip(a, b):
         assert n1 == n2 and i1 == i2 == "0"
         assert h1 == h2, f"n={n1}: look-ahead factors differ from the serial block order"
+
+
+def test_lookahead_factors_bitwise_serial_when_serialised():
+    """The same with launches serialised in issue order (the side stream's panels are issued before the
+    caller's stream applies the previous block's interchanges): the streams share no scratch they race on."""
+    a, b = _digests(True, blocking=True), _digests(False)
+    for (n1, i1, h1), (n2, i2, h2) in zip(a, b):
+        assert n1 == n2 and i1 == i2 == "0"
+        assert h1 == h2, f"n={n1}: serialised look-ahead factors differ from the serial block order"
 
 
 def test_lookahead_backward_error():

@@ -834,9 +834,9 @@ constexpr int kLookaheadCtas = kMaxPanelCtas;  // SMs kept for the look-ahead bl
 constexpr int kEarlyForkRows = 12288;
 
 size_t lu_df_workspace_bytes(int n) {
-  // panel scratch (rounded up to 256 B), the swap maps of one 256-column block's panels, the digit scratch of
+  // panel scratch (rounded up to 256 B), the swap maps of two 256-column blocks' panels, the digit scratch of
   // the trailing update and that of the look-ahead block's own updates (the two run at the same time)
-  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + size_t(kOuterNb / kLuNb) * kSwapMapInts * 4 +
+  return ((lu_panel_workspace_bytes(kLuNb) + 255) & ~size_t(255)) + 2 * size_t(kOuterNb / kLuNb) * kSwapMapInts * 4 +
          ozaki3_scratch_bytes(n, n, kOuterNb) + ozaki3_scratch_bytes(n, kOuterNb, kLuNb);
 }
 
@@ -914,7 +914,10 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
   double* diag_row = cand_row + 2ll * 1024 * nb;
   char* after = base + ((lu_panel_workspace_bytes(nb) + 255) & ~size_t(255));
   int32_t* swap_maps = reinterpret_cast<int32_t*>(after);
-  char* digits = after + size_t(kOuterNb / kLuNb) * kSwapMapInts * 4;
+  char* digits = after + 2 * size_t(kOuterNb / kLuNb) * kSwapMapInts * 4;
+  // The swap maps of block [K0, K0 + 256) sit in the half of swap_maps chosen by the block's parity: the
+  // look-ahead block's panels write their maps while the caller's stream still applies the previous block's.
+  auto block_maps = [&](int K0) { return swap_maps + ((K0 / kOuterNb) & 1) * (kOuterNb / kLuNb) * kSwapMapInts; };
   const size_t digits_bytes = ozaki3_scratch_bytes(n, n, kOuterNb);
   char* digits_la = digits + digits_bytes;
   const size_t digits_la_bytes = ozaki3_scratch_bytes(n, kOuterNb, kLuNb);
@@ -977,7 +980,7 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     int e;
     for (int k = K0, p = 0; k < KE; k += nb, ++p) {
       const int w = std::min(nb, KE - k);
-      int32_t* map = swap_maps + p * kSwapMapInts;
+      int32_t* map = block_maps(K0) + p * kSwapMapInts;
       e = launch_panel_f32(Whi, ld, n, k, w, piv, recs, map, st, us);
       if (e == UPDES_ERR_UNSUPPORTED)
         e = launch_panel<float, true>(Whi, Wlo, ld, Whi, ld, n, k, w, piv, bar, cand, cand_row, diag_row, map, st,
@@ -1010,7 +1013,7 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     if (!j.njobs) return UPDES_OK;
     const int nmaps = int(ceil_div(KE - K0, nb));
     StatScope sc(kStatOther, s, 0.0, 2.0 * 2 * nb * maxc * 4.0 * j.njobs * nmaps);
-    swap_rows_maps_kernel<<<dim3(unsigned(ceil_div(maxc, 64)), j.njobs), 256, 0, s>>>(j, ld, swap_maps, nmaps);
+    swap_rows_maps_kernel<<<dim3(unsigned(ceil_div(maxc, 64)), j.njobs), 256, 0, s>>>(j, ld, block_maps(K0), nmaps);
     UPDES_LAUNCH_CHECK();
     return UPDES_OK;
   };
