@@ -199,10 +199,11 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
 }
 
 // ---- digit pre-pass ------------------------------------------------------------------------------------
-// A (m x K, lda) -> Ad[p][r][k] (bf16, p < 3, k < Kp) and As[r][kb] = 2^(e-8), one warp per (row, k block).
-__global__ void digits_rows_kernel(const float* __restrict__ A, int64_t lda, int m, int K, int Kp,
-                                   __nv_bfloat16* __restrict__ Ad, float* __restrict__ As) {
-  const int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+// A (m x K, lda) -> Ad[p][r][k] (bf16, p < 3, k < Kp) and As[r][kb] = 2^(e-8), one warp per (row, k block);
+// bx is the block's index among the row part's blocks.
+__device__ __forceinline__ void digits_rows(int bx, const float* __restrict__ A, int64_t lda, int m, int K, int Kp,
+                                            __nv_bfloat16* __restrict__ Ad, float* __restrict__ As) {
+  const int64_t w = (int64_t(bx) * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nkb = Kp / TK;
   if (w >= int64_t(m) * nkb) return;
@@ -233,12 +234,11 @@ __global__ void digits_rows_kernel(const float* __restrict__ A, int64_t lda, int
 }
 
 // B (K x nc, ldb) -> Bd[p][c][k] (bf16, transposed) and Bs[kb][c] (row stride ncp = nc rounded up to TN, the
-// padding columns 0); a CTA per (64 k, 64 columns) tile.
-__global__ void __launch_bounds__(256) digits_cols_kernel(const float* __restrict__ B, int64_t ldb, int nc, int K,
-                                                          int Kp, __nv_bfloat16* __restrict__ Bd,
-                                                          float* __restrict__ Bs) {
+// padding columns 0); a CTA per (64 k, 64 columns) tile: column tile bx, k block kb.
+__device__ __forceinline__ void digits_cols(int bx, int kb, const float* __restrict__ B, int64_t ldb, int nc, int K,
+                                            int Kp, __nv_bfloat16* __restrict__ Bd, float* __restrict__ Bs) {
   __shared__ float t[TK][TN + 1];
-  const int kb = blockIdx.y, c0 = blockIdx.x * TN;
+  const int c0 = bx * TN;
   for (int e = threadIdx.x; e < TK * TN; e += blockDim.x) {
     const int k = e / TN, c = e % TN;
     const int gk = kb * TK + k, gc = c0 + c;
@@ -271,6 +271,22 @@ __global__ void __launch_bounds__(256) digits_cols_kernel(const float* __restric
         x = __fmul_rn(__fsub_rn(x, d), 512.f);
       }
     }
+  }
+}
+
+// Both digit passes of one update in a single launch: blocks [0, row_blocks) take the rows of A, the next
+// col_tiles x nkb blocks the (column tile, k block) tiles of B.
+__global__ void __launch_bounds__(256) digits_kernel(const float* __restrict__ A, int64_t lda, int m,
+                                                     const float* __restrict__ B, int64_t ldb, int nc, int K, int Kp,
+                                                     int row_blocks, int col_tiles, __nv_bfloat16* __restrict__ Ad,
+                                                     float* __restrict__ As, __nv_bfloat16* __restrict__ Bd,
+                                                     float* __restrict__ Bs) {
+  const int b = int(blockIdx.x);
+  if (b < row_blocks) {
+    digits_rows(b, A, lda, m, K, Kp, Ad, As);
+  } else {
+    const int q = b - row_blocks;
+    digits_cols(q % col_tiles, q / col_tiles, B, ldb, nc, K, Kp, Bd, Bs);
   }
 }
 
@@ -658,9 +674,9 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
   StatScope sc(kStatGemm, s, 2.0 * m * double(nc) * K, double(m) * nc * 16.0 + (double(m) + nc) * K * 4.0);
   {
     const int64_t warps = int64_t(m) * nkb;
-    digits_rows_kernel<<<unsigned(ceil_div(warps * 32, 256)), 256, 0, s>>>(A, lda, m, K, Kp, Ad, As);
-    UPDES_LAUNCH_CHECK();
-    digits_cols_kernel<<<dim3(unsigned(ceil_div(nc, TN)), unsigned(nkb)), 256, 0, s>>>(B, ldb, nc, K, Kp, Bd, Bs);
+    const int row_blocks = int(ceil_div(warps * 32, 256)), col_tiles = int(ceil_div(nc, TN));
+    digits_kernel<<<unsigned(row_blocks + col_tiles * nkb), 256, 0, s>>>(A, lda, m, B, ldb, nc, K, Kp, row_blocks,
+                                                                      col_tiles, Ad, As, Bd, Bs);
     UPDES_LAUNCH_CHECK();
   }
   const int ntiles = int(ceil_div(m, TM) * ceil_div(nc, TN));
