@@ -538,7 +538,8 @@ __global__ void __launch_bounds__(256) eval_values_batch_kernel(updes_problem p,
 //    once to double-float;
 //  - for a row with operator weights w (value, d/dx, d/dy, d2/dx2, d2/dy2) and k = 2a+1,
 //        K_ij = r^(k-2) (A0 r^2 + A1 dx + A2 dy + A3 + (A4 dx^2 + A5 dy^2) / r^2)
-//    with A = (w0, k w1, k w2, k (w3 + w4), k (k-2) w3, k (k-2) w4) for interior rows (the closed forms
+//    with A = (w0, k w1, k w2, k (w3 + w4), k (k-2) w3, k (k-2) w4) for interior rows (A3 + A4, 0, 0 in the
+//    last three when w3 = w4, since the last term is then A4 exactly; the closed forms
 //    phi = r^k, g1 = k r^(k-2), g2 = k (k-2) r^(k-4) of rbf_g), A = (1, 0, 0, 0, 0, 0) for Dirichlet,
 //    (0, k n1x, k n1y, 0, 0, 0) for Neumann and (beta, k n1x, k n1y, 0, 0, 0) for Robin rows; the entry is
 //    0 at r = 0 as in the FP64 kernel (phi(0) = 0, derivatives 0 there);
@@ -580,6 +581,12 @@ __global__ void assemble_df_setup_kernel(updes_problem p, DfRow* __restrict__ ro
   if (ri.kind == -1) {
     A[0] = ri.w0; A[1] = k * ri.w1; A[2] = k * ri.w2; A[3] = k * (ri.w3 + ri.w4);
     A[4] = k * (k - 2.0) * ri.w3; A[5] = k * (k - 2.0) * ri.w4;
+    // an isotropic second-order part (A4 = A5, e.g. the Laplacian): (A4 dx^2 + A5 dy^2) / r^2 = A4 exactly,
+    // folded into the constant so that the entry needs no division
+    if (A[4] == A[5]) {
+      A[3] += A[4];
+      A[4] = A[5] = 0.0;
+    }
   } else if (ri.kind == UPDES_ROW_DIRICHLET) {
     A[0] = 1.0;
   } else if (ri.kind == UPDES_ROW_NEUMANN || ri.kind == UPDES_ROW_ROBIN) {
