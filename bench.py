@@ -285,10 +285,10 @@ def run_ours(args, world, rank, local):
     roof.update({"kernel": dom, "launches": d["count"] // steps, "avg_launch_ms": d["ms"] / d["count"],
                  "algorithmic_per_launch": (d["flops"] if roof["unit"] == "TFLOP/s" else d["bytes"]) / d["count"]})
     # DRAM bytes (read + write) per algorithmic byte of the dominant kernel, from one ncu capture of the update
-    # after the first block at n = 10,006 (m = 9,750, nc = 9,494, K = 256: 1.479 GB of DRAM traffic against
-    # 1.501 GB algorithmic), scaled to this run's average launch by its algorithmic bytes (the traffic grows
-    # with the entries updated)
-    dram_per_alg_byte = {"trailing_update": 1.4787e9 / 1.5008e9}
+    # after the first block at n = 10,006 (m = 9,750, nc = 9,494, K = 256: 1.478 GB of DRAM traffic against
+    # 1.501 GB algorithmic, current kernel), scaled to this run's average launch by its algorithmic bytes (the
+    # traffic grows with the entries updated)
+    dram_per_alg_byte = {"trailing_update": 1.4777e9 / 1.5008e9}
     roof["traffic"] = dram_per_alg_byte[dom] * d["bytes"] / d["count"] if dom in dram_per_alg_byte else None
     cpu = None
     if rank == 0 and not args.no_cpu:
