@@ -1628,6 +1628,12 @@ __device__ __forceinline__ void df_fma_x2(float2 f, float2 fl, float2 xh, float2
   sl = sub2(t, sub2(sh, s0));
 }
 
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // The same triangular solve in blocks of 128 rows, one CTA of 512 threads each: the chain of blocks (an L2
 // hand-off per block) is half as long.  Off-diagonal 128 x 128 tiles are applied as in trsv_f32_kernel
 // (four threads per row, 32 columns each, two independent accumulators); each prefetched tile is stored to
@@ -1717,10 +1723,12 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
     const int c0 = tile_cols(q);
     const int cols = min(kTB2, n - c0);
     if (tid == 0 && s_done <= q) {
-      volatile int* vc = flags + nblk;
+      // acquire loads of the count of finished blocks: they synchronise with each block's fence and increment,
+      // and the CTA barrier below carries that order to the threads that then read x
+      const int* vc = flags + nblk;
       long long it = 0;
       int d;
-      while ((d = *vc) <= q) {
+      while ((d = ld_acquire_gpu(vc)) <= q) {
         if (++it > kSpinLimit) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 30 + MODE);
@@ -1729,7 +1737,6 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
         }
         __nanosleep(20);
       }
-      __threadfence();
       s_done = d;
     }
     __syncthreads();  // tile q is in sT (stored in the previous round); block q is solved
