@@ -36,10 +36,17 @@ METRIC = "solves/s at N=22.5k: FP32-LU+FP64 IR vs FP64 LU, same GB300, rel err<=
 UNIT = "solves/s"
 
 
+L2_BYTES = 129e6  # GB300's L2
+
+
 def workload_spec(nx):
+    n = nx * nx + 6
+    planes = n * (-(-n // 32) * 32) * 8  # K as two FP32 planes, rows padded to 32 elements
+    l2 = ("inputs larger than L2" if planes > L2_BYTES else "inputs smaller than L2") + \
+        f" (K's double-float planes {planes / 1e9:.2f} GB, L2 {L2_BYTES / 1e6:.0f} MB)"
     return {"workload": f"poisson_manufactured_r3_deg2_jitter0.2_N{nx * nx}", "nodes": nx * nx,
-            "n": nx * nx + 6, "rbf": "polyharmonic r^3", "max_degree": 2, "jitter": "U(-0.2h,0.2h) seed 0",
-            "facets": "all Dirichlet", "l2": "inputs larger than L2 (matrices >= 4 GB)"}
+            "n": n, "rbf": "polyharmonic r^3", "max_degree": 2, "jitter": "U(-0.2h,0.2h) seed 0",
+            "facets": "all Dirichlet", "l2": l2}
 
 
 def make_problem(nx, U):
