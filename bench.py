@@ -110,32 +110,35 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample(nx_sample, n_full):
-    """The oracle's restatement of the reference's solve (inv -> GEMM -> QR -> inv) at a bounded
-    sample size, on all host cores; scaled to the full size by (n_full / n_sample)^3."""
+def oracle_problem(nx):
+    """The workload built by the oracle alone (its cloud, rows and weights): K, A and q of the N = nx^2 system."""
     from oracle import updes_np as O
     facets = {"South": "d", "West": "d", "North": "d", "East": "d"}
-    xs = np.linspace(0, 1, nx_sample)
-    h = xs[1] - xs[0]
-    coords = np.stack(np.meshgrid(xs, xs, indexing="ij"), -1).reshape(-1, 2)
-    ii, jj = np.divmod(np.arange(nx_sample * nx_sample), nx_sample)
-    inner = (ii > 0) & (ii < nx_sample - 1) & (jj > 0) & (jj < nx_sample - 1)
-    coords[inner] += np.random.default_rng(0).uniform(-0.2 * h, 0.2 * h, size=(inner.sum(), 2))
-    t0 = time.perf_counter()
-    cl = O.square_cloud(nx_sample, nx_sample, facets, coords=coords)
+    cl = O.square_cloud(nx, nx, facets, coords=O.jitter_coords(nx, nx, facets, 0.2, 0))
     X = cl.sorted_nodes
-    W = np.zeros((cl.Ni, 5)); W[:, 3:] = 1.0
+    W = np.zeros((cl.Ni, 5))
+    W[:, 3:] = 1.0
     K = O.assemble_K(cl, "polyharmonic", 1, 2, W, O.boundary_rows(cl, {}))
     A = O.assemble_A(cl, "polyharmonic", 1, 2)
     us = np.sin(np.pi * X[:, 0]) * np.sin(np.pi * X[:, 1])
     q = np.where(np.arange(cl.N) < cl.Ni, -2 * np.pi ** 2 * us, us)
+    return K, A, q
+
+
+def cpu_solve(nx, faithful):
+    """One CPU solve of the full workload by the oracle on all host cores: assembly of K and A, then either the
+    reference's own order of operations (inv -> GEMM -> QR -> inv, updes/operators.py:602-618) or one direct
+    LU of K (a proxy with about 11x fewer flops).  Returns (seconds, assembly seconds, vals)."""
+    from oracle import updes_np as O
+    t0 = time.perf_counter()
+    K, A, q = oracle_problem(nx)
     t1 = time.perf_counter()
-    O.solve_faithful(K, A, q)
+    if faithful:
+        u = O.solve_faithful(K, A, q)[0]
+    else:
+        u = O.solve_direct(K, A, q)[0]
     t2 = time.perf_counter()
-    n_s = cl.N + 6
-    r = n_full / n_s
-    # assembly is O(n^2), the inverse / GEMM / QR O(n^3)
-    return t2 - t0, (t1 - t0) * r ** 2 + (t2 - t1) * r ** 3, n_s
+    return t2 - t0, t1 - t0, u
 
 
 def cpu_threads():
@@ -173,28 +176,41 @@ def max_over_ranks(x, world):
 
 
 def run_reference(args, world, rank):
-    """The reference's CPU path (the oracle port: the reference needs JAX, which is not installed)."""
+    """The reference's CPU path, timed at the full configuration: the oracle's restatement of its solve
+    (assembly, then inv -> GEMM -> QR -> inv, FP64 LAPACK on all host cores).  The reference itself needs JAX,
+    which is not installed.  Warm-up steps run the 600-node README configuration (they load LAPACK and start
+    its threads; a CPU path has nothing else to warm).  Timed steps run at full size until the time budget
+    (--ref-budget-s) would be exceeded by another step; the line reports the steps actually timed."""
     if rank != 0:
         return
-    n_full = args.nx * args.nx + 6
+    from oracle import updes_np as O
     for _ in range(args.warmup):
-        cpu_sample(args.sample_nx, n_full)
-    times = []
+        facets = {"South": "n", "West": "d", "North": "d", "East": "d"}
+        cl = O.square_cloud(30, 20, facets)
+        W = np.zeros((cl.Ni, 5)); W[:, 3:] = 1.0
+        O.solve_faithful(O.assemble_K(cl, "polyharmonic", 1, 1, W, O.boundary_rows(cl, {})),
+                         O.assemble_A(cl, "polyharmonic", 1, 1), np.ones(cl.N))
+    times, asm = [], []
+    t_start = time.perf_counter()
     for _ in range(args.steps):
-        dt, scaled, n_s = cpu_sample(args.sample_nx, n_full)
-        times.append(scaled)
+        dt, ta, _ = cpu_solve(args.nx, faithful=True)
+        times.append(dt)
+        asm.append(ta)
+        elapsed = time.perf_counter() - t_start
+        if elapsed + statistics.mean(times) > args.ref_budget_s:
+            break
     ms = 1000.0 * statistics.mean(times)
     value = 1000.0 / ms
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": workload_spec(args.nx),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
-                             "sample": f"oracle restatement of the reference solve (inv->GEMM->QR->inv, FP64 "
-                                       f"LAPACK) at N={args.sample_nx ** 2} (n={args.sample_nx ** 2 + 6}) per step; assembly "
-                                       f"scaled by (n/n_sample)^2 and the solve by (n/n_sample)^3 to n={n_full}; "
-                                       f"JAX is not installed, so the "
-                                       f"reference itself cannot run"},
+    sample = (f"the full configuration (N={args.nx ** 2}, n={args.nx ** 2 + 6}) solved by the oracle's restatement "
+              f"of the reference's order of operations (assembly {statistics.mean(asm):.1f} s, then "
+              f"inv -> GEMM -> QR -> inv in FP64 LAPACK), {len(times)} of {args.steps} requested steps timed "
+              f"(budget {args.ref_budget_s:.0f} s); JAX is not installed, so the reference itself cannot run")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(times),
+            "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {**workload_spec(args.nx), "timed": "full size, no extrapolation",
+                       "warmup_workload": "README Laplace N=600 (warms LAPACK's threads)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu_threads(), "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -246,23 +262,28 @@ def run_ours(args, world, rank, local):
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     v32h, v64h = v32.cpu().numpy(), v64.cpu().numpy()
 
+    # the timed region: K solves with no per-launch instrumentation (the library only counts launches)
     sampler = ClockSampler(local)
-    ms32, st32 = timed(lambda: solve_device(dp, qd, opts32), args.steps, args.warmup, with_stats=True, clocks=sampler,
+    steps = args.steps
+    ms32, st32 = timed(lambda: solve_device(dp, qd, opts32), steps, args.warmup, clocks=sampler,
                        nvtx="mixed_solve_timed")
     clocks = sampler.summary()
+    # the same K solves again with every launch bracketed by CUDA events on its stream: per-kernel times, the
+    # roofline of the dominant kernel (its events run during these solves, so it is measured live)
+    ms_prof, stp = timed(lambda: solve_device(dp, qd, opts32), steps, 0, with_stats=True)
     ms64, st64 = timed(lambda: solve_device(dp, qd, opts64), args.fp64_steps, 1)
 
-    # end to end through the public API (host arrays in, vals/coeffs out)
+    # end to end through the public API (host arrays in, vals/coeffs out), as many steps as the timed region
     def e2e_call():
         sol = U.pde_solver(op, rhs, cloud, bcs, U.polyharmonic, 2, options=opts32)
         return sol
-    ms_e2e, _ = timed(e2e_call, max(1, args.e2e_steps), 1)
+    e2e_steps = args.e2e_steps or steps
+    ms_e2e, _ = timed(e2e_call, e2e_steps, 1)
     h2d = (cloud.N * 2 * 8 + cloud.Ni * 5 * 8 + (cloud.N - cloud.Ni) * (4 * 2 + 4 + 8 * 8) + cloud.N * 8)
     d2h = cloud.N * 8 + (cloud.N + 6) * 8
 
-    steps = args.steps
     value = world * steps / (ms32 / 1000.0)
-    per = {k: v for k, v in st32["by_class"].items() if v["count"]}
+    per = {k: v for k, v in stp["by_class"].items() if v["count"]}
     dom = max(per, key=lambda k: per[k]["ms"])
     d = per[dom]
     peaks = {}
@@ -271,39 +292,63 @@ def run_ours(args, world, rank, local):
     except Exception:
         pass
     if dom == "trailing_update":
-        # The mixed path's trailing update runs on the tensor cores: each FP32 operand is written as 3 bf16
-        # integer digits, and 8 of the 3 x 3 digit products of every 2 m n K update (all but the one below
-        # the digit cut) are exact tcgen05 MMAs (9 with UPDES_OZAKI=2).
-        # achieved = tensor flops of those products / kernel time, against the measured bf16 peak (the
-        # kernel runs inside a seconds-long step: the sustained figure).
+        # achieved counts the algorithmic flops of the updates, 2 m nc K per launch (the LU's (2/3) n^3 in
+        # all), against the measured bf16 sustained peak of the tensor cores the update runs on (it runs
+        # inside a seconds-long step).  Each FP32 operand is written as 3 bf16 integer digits and 8 of the
+        # 3 x 3 digit products are exact tcgen05 MMAs (9 with UPDES_OZAKI=2): tensor_work_* count those.
         digit_products = 9 if os.environ.get("UPDES_OZAKI", "") == "2" else 8
-        achieved = digit_products * d["flops"] / (d["ms"] / 1000.0) / 1e12
+        achieved = d["flops"] / (d["ms"] / 1000.0) / 1e12
         peak = peaks.get("bf16_tflops_sustained", 1700.0)
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                 "peak_source": "of measured bf16 sustained" if "bf16_tflops_sustained" in peaks else "of fallback",
-                "digit_products": digit_products,
-                "fp64_equivalent_tflops": d["flops"] / (d["ms"] / 1000.0) / 1e12}
-        d = dict(d, flops=digit_products * d["flops"])
+                "work": "algorithmic 2*m*nc*K flops per update launch",
+                "digit_products": digit_products, "tensor_work_tflops": digit_products * achieved,
+                "tensor_work_frac": digit_products * achieved / peak}
     else:
         achieved = d["bytes"] / (d["ms"] / 1000.0) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback"}
     roof.update({"kernel": dom, "launches": d["count"] // steps, "avg_launch_ms": d["ms"] / d["count"],
-                 "algorithmic_per_launch": (d["flops"] if roof["unit"] == "TFLOP/s" else d["bytes"]) / d["count"]})
-    # DRAM bytes (read + write) per algorithmic byte of the dominant kernel, from one ncu capture of the update
-    # after the first block at n = 10,006 (m = 9,750, nc = 9,494, K = 256: 1.478 GB of DRAM traffic against
-    # 1.501 GB algorithmic, current kernel), scaled to this run's average launch by its algorithmic bytes (the
-    # traffic grows with the entries updated)
-    dram_per_alg_byte = {"trailing_update": 1.4777e9 / 1.5008e9}
-    roof["traffic"] = dram_per_alg_byte[dom] * d["bytes"] / d["count"] if dom in dram_per_alg_byte else None
+                 "algorithmic_per_launch": (d["flops"] if roof["unit"] == "TFLOP/s" else d["bytes"]) / d["count"],
+                 "algorithmic_bytes_per_launch": d["bytes"] / d["count"],
+                 "measured_in": "a second pass of the same steps with per-launch CUDA events on each launch's "
+                                "stream (the timed region itself runs without them)"})
+    # DRAM bytes (read + write) of the update per algorithmic byte (the double-float C planes read and
+    # written once plus the digit operands), from one ncu capture of the update kernel; applied to this run's
+    # average launch.  An estimate, named with its source.
+    dram_per_alg_byte = {"trailing_update": (1.4777e9 / 1.5008e9,
+                                             "ncu dram__bytes_read.sum + dram__bytes_write.sum of one update "
+                                             "launch at n = 10,006 (m = 9,750, nc = 9,494, K = 256): 1.478 GB "
+                                             "against 1.501 GB algorithmic, scaled by this run's algorithmic "
+                                             "bytes per launch")}
+    if dom in dram_per_alg_byte:
+        ratio, src = dram_per_alg_byte[dom]
+        roof["traffic"] = ratio * d["bytes"] / d["count"]
+        roof["traffic_source"] = src
+    else:
+        roof["traffic"] = None
     cpu = None
     if rank == 0 and not args.no_cpu:
-        dt, scaled, n_s = cpu_sample(args.sample_nx, args.nx * args.nx + 6)
-        cpu = {"value": 1000.0 / (scaled * 1000.0), "unit": UNIT, "cores": cpu_threads(), "kind": "port",
-               "sample": f"oracle restatement of the reference solve (inv->GEMM->QR->inv) at N={args.sample_nx ** 2}: "
-                         f"{dt:.2f} s; assembly scaled by (n/n_sample)^2, solve by (n/n_sample)^3 "
-                         f"(n/n_sample = {(args.nx ** 2 + 6) / n_s:.2f})"}
+        dt, ta, u_cpu = cpu_solve(args.nx, faithful=False)
+        cpu = {"value": 1.0 / dt, "unit": UNIT, "cores": cpu_threads(), "kind": "port",
+               "sample": f"one solve of the full configuration (N={args.nx ** 2}) on the host cores by the oracle, "
+                         f"measured, not extrapolated: assembly {ta:.1f} s + a direct FP64 LU of K "
+                         f"{dt - ta:.1f} s (a proxy: the reference's inv -> GEMM -> QR order, which "
+                         f"`--impl reference` times, costs about 11x the flops); its vals agree with the GPU's "
+                         f"mixed path to {rel(v32h, u_cpu):.1e}"}
+    acc = {"rel_err_vals_vs_fp64_lu": rel(v32h, v64h), "rel_err_vals_vs_exact": rel(v32h, us),
+           "fp64_rel_err_vs_exact": rel(v64h, us), "gmres_iters": info32["iters"],
+           "fell_back": info32["fell_back"], "backward_error": info32["backward_error"],
+           "fp64_backward_error": info64["backward_error"]}
+    gold = os.path.join(ROOT, "tests", "golden", f"full_poisson_{args.nx}.npz")
+    if os.path.exists(gold):
+        g = np.load(gold)
+        acc["rel_err_vals_vs_oracle"] = rel(v32h, g["vals"])
+        acc["fp64_rel_err_vals_vs_oracle"] = rel(v64h, g["vals"])
+        acc["oracle"] = "FP64 direct LU of K on the CPU (tests/golden/make_fullsize.py)"
+        if "vals_faithful" in g.files:
+            acc["rel_err_vals_vs_oracle_reference_order"] = rel(v32h, g["vals_faithful"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
         "ms_per_step": ms32 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -312,15 +357,13 @@ def run_ours(args, world, rank, local):
         "fp64_lu": {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": UNIT,
                     "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps},
         "speedup_vs_fp64_lu": (ms64 / args.fp64_steps) / (ms32 / steps),
-        "accuracy": {"rel_err_vals_vs_fp64_lu": rel(v32h, v64h), "rel_err_vals_vs_exact": rel(v32h, us),
-                     "fp64_rel_err_vs_exact": rel(v64h, us), "gmres_iters": info32["iters"],
-                     "fell_back": info32["fell_back"], "backward_error": info32["backward_error"],
-                     "fp64_backward_error": info64["backward_error"]},
+        "accuracy": acc,
         "phases_ms": {k: info32[k] for k in ("t_assemble_ms", "t_factor_ms", "t_refine_ms", "t_eval_ms")},
-        "e2e": {"value": world * max(1, args.e2e_steps) / (ms_e2e / 1000.0), "unit": UNIT,
+        "e2e": {"value": world * e2e_steps / (ms_e2e / 1000.0), "unit": UNIT, "steps": e2e_steps,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roof, "clocks": clocks, "gpu_launches": st32["launches"],
         "kernel_ms_per_step": {k: v["ms"] / steps for k, v in per.items()},
+        "instrumented_ms_per_step": ms_prof / steps,
         "cpu_baseline": cpu,
     }
     if rank == 0 and not args.no_extra:
@@ -466,8 +509,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nx", type=int, default=150)
     ap.add_argument("--fp64-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--sample-nx", type=int, default=70)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="end-to-end steps (default: --steps)")
+    ap.add_argument("--ref-budget-s", type=float, default=240.0,
+                    help="time budget of the reference arm's timed steps (at least one full-size step runs)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
     ap.add_argument("--adv-steps", type=int, default=500)

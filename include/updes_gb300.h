@@ -11,8 +11,7 @@
  * `info` word), and scratch memory is a caller-provided workspace whose size
  * the matching *_workspace query returns.
  *
- * Python callers bind these symbols with ctypes (updes_gb300/_lib.py); the
- * reference-side binding a maintainer would add is shown in INTEGRATION.md.
+ * Python callers bind these symbols with ctypes (updes_gb300/_lib.py).
  */
 #ifndef UPDES_GB300_H
 #define UPDES_GB300_H
@@ -199,7 +198,9 @@ UPDES_API int updes_lu_solve(int32_t n, const void* F, int64_t ldf, int32_t prec
  * Limit: n <= UPDES_NOALLOC_MAX_N; larger n returns UPDES_ERR_TOO_LARGE before
  * any GPU work.  The first call on each device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current, so make that
- * first call before any stream capture.  Every call on a device shares the
+ * first call before any stream capture (a failed lookup during capture
+ * returns UPDES_ERR_CUDA, and updes_last_error says why).  Device ordinals
+ * 64 and above return UPDES_ERR_UNSUPPORTED.  Every call on a device shares the
  * same array: calls that overlap on the GPU (different streams, or different
  * host threads) race, so order them, e.g. on one stream.  Each call clears
  * the parts that must start at zero itself.
@@ -220,7 +221,8 @@ typedef struct {
   int32_t restart;        /* GMRES restart length                                        */
   int32_t fallback_fp64;  /* 1: if refinement stalls, refactor in FP64 and solve again    */
   double tol;             /* stop when ||b - K c|| <= tol ||b||, or when the componentwise
-                             backward error reaches the FP64 floor (64 unit roundoffs)      */
+                             backward error reaches 256 FP64 unit roundoffs (what the
+                             double-float planes of K can certify)                          */
 } updes_solve_opts;
 
 typedef struct {
@@ -347,6 +349,19 @@ UPDES_API int updes_solve_transpose(const updes_problem* p, const double* g, dou
  * on the fly (no matrix is stored). */
 UPDES_API int updes_coeff_grad(const updes_problem* p, const double* coeffs, const double* lambda, double* dW,
                                void* stream);
+
+/* ---- bounded waits ---------------------------------------------------------
+ * Every spin-wait between CTAs (grid barriers, the panels' record exchange, the
+ * triangular solves' block flags) gives up after a number of polls and then
+ * reports UPDES_ERR_TIMEOUT instead of hanging; by default that is 2^26 polls
+ * (seconds).  updes_set_spin_limit sets the number of polls on the current
+ * device for every later launch of the library (0 restores the default); a
+ * caller with a watchdog of its own may shorten it.  The tensor-core update's
+ * waits on its own copies keep the default.  Not part of the reference, which
+ * has no device-side waits (its errors are Python exceptions and
+ * asserts, updes/assembly.py:474, updes/operators.py:729).
+ */
+UPDES_API int updes_set_spin_limit(int64_t iterations);
 
 /* ---- instrumentation ------------------------------------------------------ */
 

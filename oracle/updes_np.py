@@ -349,6 +349,26 @@ def boundary_rows(cloud: Cloud, robin: dict, compat: bool = True) -> BoundaryRow
 # Assembly
 # ---------------------------------------------------------------------------
 
+# Rows per block of the dense assemblies: bounds the temporaries (about 13 arrays of ROW_BLOCK x N FP64 per
+# thread) at full size.
+ROW_BLOCK = 256
+
+
+def _row_blocks(nrows, fn, threads=None):
+    """fn(r0, r1) over blocks of ROW_BLOCK rows on a thread pool (NumPy releases the GIL in its ufuncs)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    blocks = [(r0, min(nrows, r0 + ROW_BLOCK)) for r0 in range(0, nrows, ROW_BLOCK)]
+    threads = threads or min(16, os.cpu_count() or 1)
+    if len(blocks) <= 1 or threads <= 1:
+        for b in blocks:
+            fn(*b)
+        return
+    with ThreadPoolExecutor(threads) as ex:
+        for f in [ex.submit(fn, *b) for b in blocks]:
+            f.result()
+
+
 def _combine(t, w):
     """a φ + bx ∂xφ + by ∂yφ + wxx ∂xxφ + wyy ∂yyφ with per-row weights w (rows, 5)."""
     phi, gx, gy, hxx, hyy = t
@@ -373,10 +393,13 @@ def assemble_K(cloud: Cloud, kind: str, param: float, max_degree: int, op_weight
     n = N + M
     K = np.zeros((n, n))
     W = np.asarray(op_weights, dtype=np.float64).reshape(Ni, 5)
-    # interior Φ rows
-    dx = X[:Ni, 0:1] - X[None, :, 0]
-    dy = X[:Ni, 1:2] - X[None, :, 1]
-    K[:Ni, :N] = _combine(rbf_terms(kind, param, dx, dy), W)
+    # interior Φ rows, in blocks of rows on a thread pool (elementwise arithmetic: the blocking changes nothing
+    # but the size of the temporaries and the threads NumPy uses)
+    def fill(r0, r1):
+        dx = X[r0:r1, 0:1] - X[None, :, 0]
+        dy = X[r0:r1, 1:2] - X[None, :, 1]
+        K[r0:r1, :N] = _combine(rbf_terms(kind, param, dx, dy), W[r0:r1])
+    _row_blocks(Ni, fill)
     if not self_term:
         K[np.arange(Ni), np.arange(Ni)] = 0.0
     for k in range(M):
@@ -426,10 +449,12 @@ def assemble_A(cloud: Cloud, kind: str, param: float, max_degree: int,
     N = cloud.N
     M = nb_monomials(max_degree)
     A = np.zeros((N + M, N + M))
-    phi = rbf_terms(kind, param, X[:, 0:1] - X[None, :, 0], X[:, 1:2] - X[None, :, 1])[0]
+
+    def fill(r0, r1):
+        A[r0:r1, :N] = rbf_terms(kind, param, X[r0:r1, 0:1] - X[None, :, 0], X[r0:r1, 1:2] - X[None, :, 1])[0]
+    _row_blocks(N, fill)
     if not self_term:
-        phi[np.arange(N), np.arange(N)] = 0.0
-    A[:N, :N] = phi
+        A[np.arange(N), np.arange(N)] = 0.0
     for k in range(M):
         p = monomial_terms(k, X[:, 0], X[:, 1])[0]
         A[:N, N + k] = p

@@ -2,7 +2,7 @@
 
 Usage (needs the Updes source tree; JAX is replaced by ``ref_shim``):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the Updes source tree> [case ...]
 
 For every case in ``cases.CASES`` this builds the reference ``SquareCloud``
 (coordinates injected, so no RNG is shared), calls the reference's own
@@ -26,6 +26,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+sys.path.insert(1, os.path.dirname(os.path.dirname(HERE)))  # the product, for its GmshCloud check
 import ref_shim  # noqa: E402
 
 ref_shim.install()
@@ -249,15 +250,63 @@ def run_gmsh(updes):
     print(f"gmsh_dshape: N={cloud.N} {time.time() - t0:.1f}s")
 
 
+def run_ref_fixture(updes, ref_path):
+    """The reference's own unit test problem (updes/tests/test_operators.py:26-103): its GmshCloud on its mesh
+    fixture (updes/tests/data/mesh.msh, every facet Neumann), Gaussian eps = 10, degree 1, operator
+    nodal_value, rhs 12, zero Neumann values; the solution is the constant 12, whose gradient and divergence
+    the reference test checks at atol 1e-2.  Stores the reference's cloud (so the GPU test can solve on it
+    without the mesh file) and its vals, coeffs, gradients and divergences; the product's GmshCloud reads the
+    same file here and must give the same cloud."""
+    from updes_gb300.cloud import GmshCloud as ProductGmshCloud
+    t0 = time.time()
+    mesh = os.path.join(ref_path, "updes", "tests", "data", "mesh.msh")
+    facets = {"Wall": "n", "Inflow": "n", "Outflow": "n", "Blowing": "n", "Suction": "n"}
+    cloud = updes.GmshCloud(filename=mesh, facet_types=dict(facets))
+    rbf = partial(updes.gaussian, eps=10.0)
+
+    def dop(x, center=None, rbf=None, monomial=None, fields=None):
+        return updes.nodal_value(x, center, rbf, monomial)
+
+    def rop(x, centers=None, rbf=None, fields=None):
+        return 12.0
+
+    zero = lambda c: 0.0
+    bcs = {f: zero for f in facets}
+    sol = updes.pde_solver(diff_operator=dop, rhs_operator=rop, cloud=cloud, boundary_conditions=bcs, rbf=rbf,
+                           max_degree=1)
+    npy = lambda t: np.asarray(t.detach() if isinstance(t, torch.Tensor) else t, dtype=np.float64)
+    grads = npy(updes.gradient_vec(cloud.sorted_nodes, sol.coeffs, cloud.sorted_nodes, rbf))
+    field_vec = torch.stack([sol.coeffs, sol.coeffs], dim=-1)
+    divs = npy(updes.divergence_vec(cloud.sorted_nodes, field_vec, cloud.sorted_nodes, rbf))
+    mine = ProductGmshCloud(mesh, facet_types=dict(facets))
+    assert np.array_equal(mine.sorted_nodes, npy(cloud.sorted_nodes))
+    assert mine.facet_nodes == {f: [int(i) for i in v] for f, v in cloud.facet_nodes.items()}
+    assert np.allclose(mine.sorted_outward_normals, npy(cloud.sorted_outward_normals), rtol=0, atol=1e-12)
+    np.savez_compressed(os.path.join(HERE, "ref_test_operators_mesh.npz"), facets=json.dumps(facets),
+                        sorted_nodes=npy(cloud.sorted_nodes), sorted_outward_normals=npy(cloud.sorted_outward_normals),
+                        counts=np.array([cloud.N, cloud.Ni, cloud.Nd, cloud.Nn, cloud.Nr], np.int64),
+                        facet_nodes=json.dumps({f: [int(i) for i in v] for f, v in cloud.facet_nodes.items()}),
+                        node_types=json.dumps({int(k): v for k, v in cloud.node_types.items()}),
+                        vals=npy(sol.vals), coeffs=npy(sol.coeffs), grads=grads, divs=divs,
+                        product_cloud_checked=np.array(True))
+    print(f"ref_test_operators_mesh: N={cloud.N} max |grad| {np.abs(grads).max():.2e} "
+          f"max |div| {np.abs(divs).max():.2e} {time.time() - t0:.1f}s")
+
+
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <path of the Updes source tree> [case ...]")
+    ref = sys.argv[1]
     updes = load_reference(ref)
-    only = sys.argv[2:] or list(C.CASES) + list(C.MULTI_CASES) + ["gmsh"]
+    only = sys.argv[2:] or list(C.CASES) + list(C.MULTI_CASES) + ["gmsh", "ref_fixture"]
     for name in only:
         if name == "adjoint":
             continue
         if name == "gmsh":
             run_gmsh(updes)
+            continue
+        if name == "ref_fixture":
+            run_ref_fixture(updes, ref)
             continue
         if name in C.MULTI_CASES:
             run_multi(updes, name, C.MULTI_CASES[name])

@@ -59,3 +59,26 @@ def assemble(dp, fp32=False):
     _lib.check(st, "updes_assemble")
     torch.cuda.synchronize()
     return K64, K32, ld
+
+
+def lu_factor_random(n, precision, seed):
+    """LU (updes_lu_factor) of a random n x n matrix + 0.5 I; returns (A, factors, ld, piv, workspace, stream)."""
+    import torch
+    lib = _lib.load()
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal((n, n)) + 0.5 * np.eye(n)
+    ld = int(lib.updes_matrix_ld(n, 8))
+    Ad = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+    Ad[:, :n] = torch.as_tensor(A)
+    F = torch.zeros((n, ld), dtype=torch.float32, device="cuda") if precision else Ad
+    piv = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    nb = ctypes.c_size_t()
+    _lib.check(lib.updes_lu_workspace(n, precision, ctypes.byref(nb)), "updes_lu_workspace")
+    ws = torch.empty(nb.value + 8 * n * 4 + 1024, dtype=torch.uint8, device="cuda")
+    info = ctypes.c_int32(-1)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.updes_lu_factor(n, Ad.data_ptr(), ld, precision, F.data_ptr() if precision else None,
+                                   ld if precision else 0, piv.data_ptr(), ws.data_ptr(), ws.numel(),
+                                   ctypes.byref(info), s), "updes_lu_factor")
+    assert info.value == 0
+    return A, F, ld, piv, ws, s

@@ -41,7 +41,7 @@ def test_reference_arm_under_torchrun_gloo():
     port = 29500 + os.getpid() % 400
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus",
-           "2", "--steps", "1", "--warmup", "3", "--sample-nx", "12"]
+           "2", "--steps", "1", "--warmup", "3", "--nx", "12"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -50,10 +50,12 @@ def test_reference_arm_under_torchrun_gloo():
 
 def test_reference_arm_line_contract():
     """One process: the reference arm's JSON line carries the contract's keys, with the CPU baseline and an
-    end-to-end entry that moves no host/device bytes, and the timing rule's floor of 3 warm-up steps."""
+    end-to-end entry that moves no host/device bytes, and the timing rule's floor of 3 warm-up steps.  The
+    steps are timed at the configuration's own size (no extrapolation); with a zero time budget exactly one
+    of the requested steps runs, and the line says so."""
     import json
-    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
-           "--sample-nx", "12", "--nx", "20"]
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "4", "--warmup", "0",
+           "--nx", "20", "--ref-budget-s", "0"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -63,6 +65,8 @@ def test_reference_arm_line_contract():
                 "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
         assert key in d, key
     assert d["impl"] == "reference" and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] >= 3
+    assert d["steps_requested"] == 4 and d["config"]["timed"] == "full size, no extrapolation"
+    assert "N=400" in d["cpu_baseline"]["sample"] and "1 of 4" in d["cpu_baseline"]["sample"]
     assert d["value"] > 0 and d["higher_is_better"] is True and d["unit"] == "solves/s"
     assert abs(d["ms_per_step"] - 1000.0 / d["value"]) < 1e-6 * d["ms_per_step"]
     cb = d["cpu_baseline"]

@@ -12,31 +12,10 @@ import ctypes
 import numpy as np
 import pytest
 
+from gpu_helpers import lu_factor_random as _factor
 from updes_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
-
-
-def _factor(n, precision, seed):
-    import torch
-    lib = _lib.load()
-    rng = np.random.default_rng(seed)
-    A = rng.standard_normal((n, n)) + 0.5 * np.eye(n)
-    ld = int(lib.updes_matrix_ld(n, 8))
-    Ad = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
-    Ad[:, :n] = torch.as_tensor(A)
-    F = torch.zeros((n, ld), dtype=torch.float32, device="cuda") if precision else Ad
-    piv = torch.empty(2 * n, dtype=torch.int32, device="cuda")
-    nb = ctypes.c_size_t()
-    _lib.check(lib.updes_lu_workspace(n, precision, ctypes.byref(nb)), "updes_lu_workspace")
-    ws = torch.empty(nb.value + 8 * n * 4 + 1024, dtype=torch.uint8, device="cuda")
-    info = ctypes.c_int32(-1)
-    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    _lib.check(lib.updes_lu_factor(n, Ad.data_ptr(), ld, precision, F.data_ptr() if precision else None,
-                                   ld if precision else 0, piv.data_ptr(), ws.data_ptr(), ws.numel(),
-                                   ctypes.byref(info), s), "updes_lu_factor")
-    assert info.value == 0
-    return A, F, ld, piv, ws, s
 
 
 @pytest.mark.parametrize("precision", [0, 1])
@@ -62,6 +41,32 @@ def test_noalloc_solve_matches_workspace_solve(precision, nrhs):
         # and both agree with the true solution as closely as the factors allow
         want = np.linalg.solve(A.T if trans else A, B)
         assert np.linalg.norm(ref - want) <= (1e-10 if precision == 0 else 1e-3) * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("n,nrhs,ldb", [(700, 2, 5), (_lib.NOALLOC_MAX_N - 37, 2, 3)])
+def test_noalloc_strided_columns_and_sizes_near_the_limit(n, nrhs, ldb):
+    """Right-hand sides that are columns of a wider row-major block (ldb > nrhs) go through the scratch's
+    column vector; the largest sizes (not a multiple of the 64-row blocks) fill its flag region.  Both
+    against the workspace-based solve, twice in a row, with the block's other columns left untouched."""
+    import torch
+    lib = _lib.load()
+    A, F, ld, piv, ws, s = _factor(n, 1, 31)
+    B = np.random.default_rng(7).standard_normal((n, ldb))
+    for trans in (0, 1):
+        Bref = torch.as_tensor(B.copy(), device="cuda")
+        _lib.check(lib.updes_lu_solve(n, F.data_ptr(), ld, 1, piv.data_ptr(), Bref.data_ptr(), nrhs, ldb, trans,
+                                      ws.data_ptr(), ws.numel(), s), "updes_lu_solve")
+        ref = Bref.cpu().numpy()
+        for call in range(2):
+            Bd = torch.as_tensor(B.copy(), device="cuda")
+            st = lib.updes_lu_solve_noalloc(n, F.data_ptr(), ld, 1, piv.data_ptr(), Bd.data_ptr(), nrhs, ldb,
+                                            trans, s)
+            assert st == _lib.OK, _lib.status_string(st)
+            got = Bd.cpu().numpy()
+            assert np.linalg.norm(got[:, :nrhs] - ref[:, :nrhs]) <= 1e-12 * np.linalg.norm(ref[:, :nrhs]), (trans, call)
+            np.testing.assert_array_equal(got[:, nrhs:], B[:, nrhs:])
+    del A, F, ws
+    torch.cuda.empty_cache()
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():

@@ -119,9 +119,15 @@ SIGNATURES = {
     "updes_solve_transpose": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),
     "updes_coeff_grad": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp, _vp]),
+    "updes_set_spin_limit": (ctypes.c_int, [_i64]),
     "updes_stats_reset": (None, [_i32]),
     "updes_stats_read": (None, [ctypes.POINTER(Stats)]),
 }
+
+
+def set_spin_limit(iterations: int = 0) -> None:
+    """Polls before a wait between CTAs gives up with ERR_TIMEOUT, on the current device (0: the default)."""
+    check(load().updes_set_spin_limit(int(iterations)), "updes_set_spin_limit")
 
 
 def stats_reset(timing: bool = False) -> None:

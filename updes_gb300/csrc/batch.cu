@@ -215,7 +215,7 @@ __device__ __forceinline__ void trsm_block(const float* __restrict__ Fh, const f
       long long it = 0;
       int d;
       while ((d = *vc) <= q) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 30);
           d = q + 1;

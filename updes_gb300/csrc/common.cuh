@@ -60,8 +60,24 @@ __device__ __forceinline__ void status_error(DeviceStatus* st, int code) {
 
 __host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
-// Iteration cap of every spin-wait (each iteration also sleeps ~64 ns): a few seconds at most.
-constexpr long long kSpinLimit = 1ll << 26;
+// Iteration cap of the spin-waits between CTAs (grid barriers, panel records, triangular-solve flags; each
+// iteration also sleeps 20-64 ns): a few seconds at most by default.  updes_set_spin_limit changes it at run
+// time on the current device.  Without relocatable device code every translation unit holds its own copy
+// of the variable, so each unit registers a setter for its copy (below) and that call runs all of them.
+constexpr long long kDefaultSpinLimit = 1ll << 26;
+static __device__ long long g_spin_limit = kDefaultSpinLimit;
+__device__ __forceinline__ long long spin_limit() { return g_spin_limit; }
+
+// Iteration cap of the tensor-core update's mbarrier waits.  It stays a constant: when such a wait gives up,
+// the kernel still waits for its own copies in flight before it leaves, and that wait must be long enough
+// for the copies to land whatever limit a caller sets for the waits between CTAs.
+constexpr long long kTcSpinLimit = kDefaultSpinLimit;
+
+int register_spin_limit_setter(int (*setter)(long long));
+namespace {
+inline int set_unit_spin_limit(long long v) { return int(cudaMemcpyToSymbol(g_spin_limit, &v, sizeof(v))); }
+const int g_spin_setter_registered = register_spin_limit_setter(&set_unit_spin_limit);
+}  // namespace
 
 // Grid-wide barrier for a cooperative launch (all CTAs co-resident).
 // `bar` points at two words: arrival count and generation.  Returns false if
@@ -81,9 +97,10 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int nbl
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
+      const long long lim = spin_limit();
       long long it = 0;
       while (*vgen == gen) {
-        if (++it > kSpinLimit) {
+        if (++it > lim) {
           ok = 0;
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, tag);

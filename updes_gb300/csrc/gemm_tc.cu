@@ -113,7 +113,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
 }
 
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
-  for (long long it = 0; it < kSpinLimit; ++it) {
+  for (long long it = 0; it < kTcSpinLimit; ++it) {
     if (mbar_try_wait(bar, phase)) return true;
     __nanosleep(32);
   }

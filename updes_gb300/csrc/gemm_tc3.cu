@@ -118,7 +118,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 
 // Bounded wait; gives up when the abort flag is raised by another role.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, volatile int* abort_flag) {
-  for (long long it = 0; it < kSpinLimit; ++it) {
+  for (long long it = 0; it < kTcSpinLimit; ++it) {
     if (mbar_try_wait(bar, phase)) return true;
     if ((it & 63) == 63 && *abort_flag) return false;
     if (it > 256) __nanosleep(32);

@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(void* W, const flo
       volatile unsigned long long* tw = reinterpret_cast<volatile unsigned long long*>(&(cand + par * G + w)->idx);
       long long it = 0;
       while (int((*tw) >> 32) != diag + 1) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 1);
           break;
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
       ulonglong2 h = ld_tagged_pair(hp);
       long long it = 0;
       while (unsigned(h.x >> 32) != want || (tid < G && unsigned(h.y >> 32) != want)) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 2);
           gave_up = true;
@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(kPanelF32Threads) panel_f32_kernel(float* W, i
       unsigned long long x = ld_tagged_cg(q);
       long long it = 0;
       while (unsigned(x >> 32) != want) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 3);
           gave_up = true;
@@ -1263,7 +1263,7 @@ __global__ void __launch_bounds__(256) trsv_kernel(const TF* __restrict__ F, int
       long long it = 0;
       int d;
       while ((d = *vc) <= q) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 10 + MODE);
           d = q + 1;
@@ -1526,7 +1526,7 @@ __global__ void __launch_bounds__(256) trsv_f32_kernel(const float* __restrict__
       long long it = 0;
       int d;
       while ((d = *vc) <= q) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 20 + MODE);
           d = q + 1;
@@ -1729,7 +1729,7 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
       long long it = 0;
       int d;
       while ((d = ld_acquire_gpu(vc)) <= q) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit()) {
           status_error(st, UPDES_ERR_TIMEOUT);
           atomicCAS(&st->timeout_tag, 0, 30 + MODE);
           d = q + 1;

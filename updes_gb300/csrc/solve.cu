@@ -1235,15 +1235,30 @@ std::mutex g_noalloc_mu;
 constexpr int kMaxDevices = 64;
 void* g_noalloc_addr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once per device).
-int noalloc_scratch(void** out) {
+// Device address of g_noalloc_scratch on the current device (looked up once per device, by the first call
+// there).  Devices with ordinal 64 or more are not supported; a lookup that fails while `s` is being captured
+// says so, since that first call has to be made outside capture.
+int noalloc_scratch(void** out, cudaStream_t s) {
   int dev = 0;
   UPDES_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return UPDES_ERR_UNSUPPORTED;
+  if (dev < 0 || dev >= kMaxDevices) {
+    updes_set_last_cuda_error(cudaErrorInvalidDevice, "updes_lu_solve_noalloc supports device ordinals 0..63",
+                              __FILE__, __LINE__);
+    return UPDES_ERR_UNSUPPORTED;
+  }
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_addr[dev]) {
     void* p = nullptr;
-    UPDES_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      const bool capturing = cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+      updes_set_last_cuda_error(e, capturing ? "cudaGetSymbolAddress(g_noalloc_scratch) during stream capture: make "
+                                               "the first updes_lu_solve_noalloc call on a device before any capture"
+                                             : "cudaGetSymbolAddress(g_noalloc_scratch)",
+                                __FILE__, __LINE__);
+      return UPDES_ERR_CUDA;
+    }
     g_noalloc_addr[dev] = p;
   }
   *out = g_noalloc_addr[dev];
@@ -1257,8 +1272,9 @@ extern "C" int updes_lu_solve_noalloc(int32_t n, const void* F, int64_t ldf, int
   if (n <= 0 || !F || ldf < n || !piv || !b || nrhs <= 0 || ldb < nrhs) return UPDES_ERR_INVALID;
   if (precision != UPDES_PREC_FP64 && precision != UPDES_PREC_FP32) return UPDES_ERR_INVALID;
   if (n > UPDES_NOALLOC_MAX_N) return UPDES_ERR_TOO_LARGE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
   void* base = nullptr;
-  int e = noalloc_scratch(&base);
+  int e = noalloc_scratch(&base, s);
   if (e) return e;
   char* c = static_cast<char*>(base);
   LuWs w{};
@@ -1266,7 +1282,6 @@ extern "C" int updes_lu_solve_noalloc(int32_t n, const void* F, int64_t ldf, int
   w.sync = reinterpret_cast<int*>(c + kNoallocSyncOff);
   w.tmp = reinterpret_cast<double*>(c + kNoallocVecOff);
   double* col = w.tmp + UPDES_NOALLOC_MAX_N;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   UPDES_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DeviceStatus), s));  // the flags are cleared by each solve
   for (int j = 0; j < nrhs; ++j) {
     double* bj = b + j;

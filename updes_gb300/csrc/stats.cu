@@ -80,3 +80,33 @@ extern "C" void updes_stats_read(updes_stats* out) {
     out->bytes[i] = g_bytes[i];
   }
 }
+
+// ---- run-time limit of the spin-waits between CTAs ------------------------------------------------------
+
+namespace {
+std::mutex g_spin_mu;
+std::vector<int (*)(long long)>& spin_setters() {
+  static std::vector<int (*)(long long)> v;  // constructed on first use: registration runs at load time
+  return v;
+}
+}  // namespace
+
+int register_spin_limit_setter(int (*setter)(long long)) {
+  std::lock_guard<std::mutex> lk(g_spin_mu);
+  spin_setters().push_back(setter);
+  return 0;
+}
+
+extern "C" int updes_set_spin_limit(int64_t iterations) {
+  if (iterations < 0) return UPDES_ERR_INVALID;
+  const long long v = iterations == 0 ? kDefaultSpinLimit : (long long)iterations;
+  std::lock_guard<std::mutex> lk(g_spin_mu);
+  for (auto fn : spin_setters()) {
+    const cudaError_t e = cudaError_t(fn(v));
+    if (e != cudaSuccess) {
+      updes_set_last_cuda_error(e, "cudaMemcpyToSymbol(g_spin_limit)", __FILE__, __LINE__);
+      return UPDES_ERR_CUDA;
+    }
+  }
+  return UPDES_OK;
+}

@@ -656,8 +656,10 @@ def prepare(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max_de
     fields = None
     if diff_args:
         fields = np.stack([np.asarray(a, dtype=np.float64) for a in diff_args])  # (F, N)
+        _require_finite(fields, "diff_args")
     W = capture_operator(diff_operator, X[:Ni], rbf, None if fields is None else fields[:, :Ni]) if Ni else \
         np.zeros((0, 5))
+    _require_finite(W, "the captured operator weights")
     q_vals, robin = _bc_values_and_betas(boundary_conditions, cloud, opts.compat_reference_quirks)
     kind, bnodes, geom = boundary_rows(cloud, robin, opts.compat_reference_quirks)
     # rhs (updes/assembly.py:434-485)
@@ -680,7 +682,17 @@ def prepare(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max_de
             q[:Ni] = [float(np.asarray(rhs_operator(Xi[i], X, rbf, fc))) for i in range(Ni)]
     for f, v in q_vals.items():
         q[np.asarray(cloud.facet_nodes[f], dtype=np.int64)] = v
+    _require_finite(q, "the right-hand side (rhs_operator and boundary values)")
+    _require_finite(geom, "the Robin coefficients")
     return W, kind, bnodes, geom, q
+
+
+def _require_finite(a, what):
+    """NaN or inf in a problem's data is rejected before any GPU work (the reference would return NaN)."""
+    a = np.asarray(a)
+    if a.size and not np.all(np.isfinite(a)):
+        bad = int(np.size(a) - np.count_nonzero(np.isfinite(a)))
+        raise ValueError(f"{what}: {bad} entries are not finite (NaN or inf)")
 
 
 def pde_solver(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max_degree, diff_args=None,
