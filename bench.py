@@ -372,6 +372,24 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def profile_solve(args):
+    """One mixed-precision solve of the workload and nothing else (no warm-up, no FP64 solve), so that a
+    profiler sees the solve's launches first: ncu -k regex:<kernel> -c 1 then captures the kernel's first
+    launch, e.g. the trailing update after the first 256-column block."""
+    import torch
+
+    import updes_gb300 as U
+    from updes_gb300.operators import DeviceProblem, SolverOptions, prepare, solve_device
+    cloud, op, rhs, bcs, _ = make_problem(args.nx, U)
+    o = SolverOptions(precision="fp32", reuse_factorization=False)
+    W, kind, bnodes, geom, q = prepare(op, rhs, cloud, bcs, U.polyharmonic, 2, options=o)
+    dp = DeviceProblem(cloud, U.polyharmonic, 2, W, kind, bnodes, geom)
+    _, _, info = solve_device(dp, torch.as_tensor(q, device="cuda"), o)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_solve": {"n": dp.n, **{k: info[k] for k in ("iters", "fell_back", "converged",
+                                                                            "backward_error")}}}), flush=True)
+
+
 def extra_configs(args, U, torch):
     """The other benchmark configurations, each bounded to seconds, measured with CUDA events (device work)
     on the current stream or the wall clock around a synchronised call (noted per entry).  A configuration
@@ -408,7 +426,10 @@ def _cfg_readme(args, U, torch):
 
 
 def _cfg_advection(args, U, torch):
-    """Advection-diffusion, N = 6,400, 64 bumps, implicit steps replayed from a CUDA graph."""
+    """Advection-diffusion, N = 6,400, 64 bumps, implicit steps replayed from a CUDA graph.  The factors are
+    FP64 (computed once), applied in double-float with one refinement sweep: the configuration names FP32 LU
+    factors, but classical refinement on FP32 factors diverges on this system (the first step's error
+    against the oracle grows from 4e1 after 4 sweeps to 1e13 after 16, GPU measurement)."""
     from updes_gb300 import workloads as WL
     from updes_gb300.multirhs import MultiRHSSolver
     stream = torch.cuda.current_stream()
@@ -431,10 +452,12 @@ def _cfg_advection(args, U, torch):
     torch.cuda.synchronize()
     solver.check_status()
     ms = e0.elapsed_time(e1) / steps
-    return {"advection_diffusion_N6400_R64": {
+    return {"advection_diffusion_N6400_R64_fp64_factors": {
         "metric": "column-solves/s (64 right-hand sides per implicit step, graph replay, CUDA events)",
         "value": 64 * 1000.0 / ms, "ms_per_step": ms, "steps": steps, "factor_setup_s": setup_s,
-        "factors": "FP64, applied as double-float planes, one refinement sweep"}}
+        "factors": "FP64 factors (not the FP32 LU the configuration names: classical refinement on FP32 factors "
+                   "diverges on this system), applied in double-float, one refinement sweep per step; the first "
+                   "step is within 1e-9 of the oracle (GPU test)"}}
 
 
 def _cfg_control(args, U, torch):
@@ -516,7 +539,12 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
     ap.add_argument("--adv-steps", type=int, default=500)
     ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="run one mixed solve and exit (the launch order a profiler capture expects)")
     args = ap.parse_args()
+    if args.profile_solve:
+        profile_solve(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup(args)

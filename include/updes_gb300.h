@@ -79,12 +79,20 @@ typedef struct {
   int32_t rbf;                /* UPDES_RBF_*                                          */
   double rbf_param;           /* a (polyharmonic, thin plate) or eps                  */
   int32_t self_term;          /* 0 = the reference's zero diagonal in Phi blocks      */
-  int32_t reserved;
+  int32_t support_width;      /* 0: every node's support is all other nodes ("max");
+                                 S > 0: local supports, S = support_size - 1 nodes each */
   const double* nodes;        /* device, N x 2, (x, y) per node                       */
   const double* op_weights;   /* device, Ni x 5: value, d/dx, d/dy, d2/dx2, d2/dy2    */
   const int32_t* bd_kind;     /* device, N - Ni: UPDES_ROW_*                          */
   const int32_t* bd_node;     /* device, (N - Ni) x 2: evaluation node, partner node  */
   const double* bd_geom;      /* device, (N - Ni) x 8: n1x n1y n2x n2y nPx nPy beta 0 */
+  const int32_t* supports;    /* device, N x support_width node ids (NULL when 0): the
+                                 support of node i (updes/cloud.py:83-112).  A row of
+                                 a Phi block keeps only its node's support columns (both
+                                 nodes' on a periodic row; updes/assembly.py:20-32,
+                                 125-128, 169-258); the P and P^T blocks stay dense.
+                                 Not supported by the batched and double-float entry
+                                 points (they return UPDES_ERR_UNSUPPORTED).          */
 } updes_problem;
 
 /* Library version (major*10000 + minor*100 + patch). */

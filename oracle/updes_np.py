@@ -241,6 +241,38 @@ def square_cloud(Nx: int, Ny: int, facet_types: dict, coords=None) -> Cloud:
     return c
 
 
+def local_supports(sorted_nodes: np.ndarray, support_size: int) -> np.ndarray:
+    """Local supports (updes/cloud.py:83-112): for every node the support_size nearest nodes by Euclidean
+    distance, the first of them (the node itself) dropped; (N, support_size - 1) node ids in sorted order.
+    The reference queries a BallTree on the original numbering and renumbers the result; distances do not
+    depend on the numbering, so the sets agree wherever no two candidates tie at the edge of a support."""
+    from scipy.spatial import cKDTree
+    N = sorted_nodes.shape[0]
+    assert 0 < support_size <= N, "support size must lie in [1, N] (updes/cloud.py:99-100)"
+    _, nb = cKDTree(sorted_nodes).query(sorted_nodes, k=support_size)
+    nb = np.asarray(nb, dtype=np.int64).reshape(N, support_size)
+    return nb[:, 1:].copy()
+
+
+def _support_mask(cloud: Cloud, supports, rows=None) -> np.ndarray:
+    """(N, N) mask of the Phi columns each of the first N rows keeps: row i of an interior, Dirichlet, Neumann
+    or Robin row (node a) keeps S(a); a periodic row (nodes a, b) keeps S(a) and S(b)
+    (updes/assembly.py:20-32, 125-128, 169-258)."""
+    N = cloud.N
+    mask = np.zeros((N, N), dtype=bool)
+    r = np.repeat(np.arange(N), supports.shape[1])
+    mask[r, supports.reshape(-1)] = True
+    if rows is not None:
+        Ni = cloud.Ni
+        for k in range(N - Ni):
+            if rows.kind[k] in (ROW_PD, ROW_PN):
+                a, b = rows.i1[k], rows.i2[k]
+                mask[Ni + k] = False
+                mask[Ni + k, supports[a]] = True
+                mask[Ni + k, supports[b]] = True
+    return mask
+
+
 def jitter_coords(Nx: int, Ny: int, facet_types: dict, frac: float, seed: int) -> np.ndarray:
     """Grid coordinates (original-id order) with U(-frac*h, +frac*h) jitter on the nodes the
     reference jitters (type not in d/n/r, updes/cloud.py:441), h = min grid spacing.
@@ -377,7 +409,7 @@ def _combine(t, w):
 
 
 def assemble_K(cloud: Cloud, kind: str, param: float, max_degree: int, op_weights,
-               rows: BoundaryRows, self_term: bool = False) -> np.ndarray:
+               rows: BoundaryRows, self_term: bool = False, supports=None) -> np.ndarray:
     """Augmented Kansa matrix K (n × n, n = N + M).
 
     Rows 0..Ni-1: interior operator rows opΦ | opP (assembly.py:93-137);
@@ -439,11 +471,13 @@ def assemble_K(cloud: Cloud, kind: str, param: float, max_degree: int, op_weight
     # Pᵀ rows
     for k in range(M):
         K[N + k, :N] = monomial_terms(k, X[:, 0], X[:, 1])[0]
+    if supports is not None:  # local supports: each row keeps the Phi columns of its support(s)
+        K[:N, :N] *= _support_mask(cloud, supports, rows)
     return K
 
 
 def assemble_A(cloud: Cloud, kind: str, param: float, max_degree: int,
-               self_term: bool = False) -> np.ndarray:
+               self_term: bool = False, supports=None) -> np.ndarray:
     """A = [[Φ, P], [Pᵀ, 0]] with Φ_ii = 0 (updes/assembly.py:10-85)."""
     X = cloud.sorted_nodes
     N = cloud.N
@@ -455,6 +489,8 @@ def assemble_A(cloud: Cloud, kind: str, param: float, max_degree: int,
     _row_blocks(N, fill)
     if not self_term:
         A[np.arange(N), np.arange(N)] = 0.0
+    if supports is not None:
+        A[:N, :N] *= _support_mask(cloud, supports)
     for k in range(M):
         p = monomial_terms(k, X[:, 0], X[:, 1])[0]
         A[:N, N + k] = p
@@ -503,9 +539,9 @@ def solve_direct(K: np.ndarray, A: np.ndarray, q: np.ndarray):
 
 
 def eval_values(cloud: Cloud, kind: str, param: float, max_degree: int, c: np.ndarray,
-                self_term: bool = False) -> np.ndarray:
+                self_term: bool = False, supports=None) -> np.ndarray:
     """u = [Φ P] c at the nodes with Φ_ii = 0 (the product's regenerate-GEMV)."""
-    return assemble_A(cloud, kind, param, max_degree, self_term)[:cloud.N] @ c
+    return assemble_A(cloud, kind, param, max_degree, self_term, supports=supports)[:cloud.N] @ c
 
 
 def value(xs, coeffs, centers, kind, param):
@@ -550,8 +586,8 @@ def laplacian(xs, coeffs, centers, kind, param):
     return out
 
 
-def field_coefficients(cloud: Cloud, kind: str, param: float, max_degree: int, values) -> np.ndarray:
+def field_coefficients(cloud: Cloud, kind: str, param: float, max_degree: int, values, supports=None) -> np.ndarray:
     """c = inv(A) [values; 0] (updes/assembly.py:404-430)."""
-    A = assemble_A(cloud, kind, param, max_degree)
+    A = assemble_A(cloud, kind, param, max_degree, supports=supports)
     M = A.shape[0] - cloud.N
     return np.linalg.solve(A, np.concatenate([np.asarray(values, dtype=np.float64), np.zeros(M)]))

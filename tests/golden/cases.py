@@ -141,6 +141,29 @@ CASES = {
                                rhs="sinsin"),
 }
 
+# Local supports (support_size an int, updes/cloud.py:83-112): each node's support is its support_size - 1
+# nearest other nodes, and every Phi block keeps only those columns (the reference's "RBF-FD" clouds).  The
+# clouds are jittered, so no two candidates tie at the edge of a support.
+LOCAL_CASES = {
+    "poisson_local_12x12": dict(Nx=12, Ny=12, facets={"South": "d", "West": "d", "North": "d", "East": "d"},
+                                rbf=("polyharmonic", 1), max_degree=1, jitter=(0.2, 21), op="laplacian",
+                                bc={"South": "sinsin", "West": "sinsin", "North": "sinsin", "East": "sinsin"},
+                                rhs="poisson_rhs", support=20),
+    "gaussian_dnr_local_11x10": dict(Nx=11, Ny=10, facets={"South": "n", "West": "n", "North": "d", "East": "r"},
+                                     rbf=("gaussian", 3.0), max_degree=2, jitter=(0.2, 23), op="helmholtz_x",
+                                     bc={"South": "zero", "West": "ylin", "North": "xsq", "East": ("ylin", "beta2")},
+                                     rhs="one", support=16),
+    "kgrad_local_10x10": dict(Nx=10, Ny=10, facets={"South": "d", "West": "d", "North": "d", "East": "d"},
+                              rbf=("polyharmonic", 2), max_degree=2, jitter=(0.2, 25), op="kgrad", fields="kfield",
+                              bc={"South": "zero", "West": "zero", "North": "sinpix", "East": "zero"},
+                              rhs="zero", support=22),
+    "periodic_local_10x9": dict(Nx=10, Ny=9, facets={"North": "p1", "South": "p1", "West": "d", "East": "d"},
+                                rbf=("multiquadric", 1.5), max_degree=1, jitter=(0.2, 27), op="laplacian",
+                                bc={"North": "zero", "South": "zero", "West": "zero", "East": "one"},
+                                rhs="one", support=12),
+}
+LOCAL_ADJOINT_CASE = "kgrad_local_10x10"
+
 # Cases whose matrices are stored in full (the others store a row subset + row checksums).
 FULL_MATRIX_MAX_N = 150
 ROW_STRIDE = 7

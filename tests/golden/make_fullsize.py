@@ -18,7 +18,12 @@ the same problem instead of against another GPU path:
 * ``control``   (``full_control_100.npz``): the N = 10,000 boundary-control
   problem (div(k grad u), r^5, degree 2) for the first of its 32 seeded
   controls: J, dJ/dc and dJ/d(fields) by a dense FP64 adjoint
-  (lambda = K^-T g on SciPy's LU, dJ/dW_i = -lambda_i (D c)_i).
+  (lambda = K^-T g on SciPy's LU, dJ/dW_i = -lambda_i (D c)_i), twice: on
+  the plain LU of K, on the LU of K equilibrated by powers of two, and on
+  the LU of K with every entry moved by up to one unit in the last place.
+  This r^5 system is so ill-conditioned that these backward-stable FP64
+  solves disagree at the 1e-3 to 1e-2 level; that distance is the problem's
+  FP64 floor, against which a GPU result is judged.
 * ``advection`` (``full_advection_80.npz``): the first implicit-Euler step of
   the N = 6,400 advection-diffusion problem for its 64 seeded bumps: the
   values of 8 columns in full and, for all 64, their norms and their dot
@@ -97,29 +102,50 @@ def control():
     north = np.asarray(cl.facet_nodes["North"], dtype=np.int64)
     q = np.zeros(N)
     q[north] = ctl
-    lu = sla.lu_factor(K)
-    c = sla.lu_solve(lu, np.concatenate([q, np.zeros(M)]))
-    u = A[:N] @ c
-    J = np.mean((u[:Ni] - ut[:Ni]) ** 2) + 1e-4 * np.sum(ctl ** 2)
-    dJdu = np.zeros(N)
-    dJdu[:Ni] = 2.0 * (u[:Ni] - ut[:Ni]) / Ni
-    g = A[:N].T @ dJdu
-    lam = sla.lu_solve(lu, g, trans=1)
-    dJ_dc = lam[north] + 2e-4 * ctl
-    dW = np.zeros((Ni, 5))
+    b = np.concatenate([q, np.zeros(M)])
+    D = []
     for kk in range(1, 5):
         e = np.zeros((Ni, 5))
         e[:, kk] = 1.0
-        Dk = O.assemble_K(cl, "polyharmonic", 2, 2, e, rows)[:Ni]
-        dW[:, kk] = -lam[:Ni] * (Dk @ c)
-        del Dk
-    dJ_dfields = np.zeros((3, N))
-    dJ_dfields[0, :Ni] = dW[:, 3] + dW[:, 4]
-    dJ_dfields[1, :Ni] = dW[:, 1]
-    dJ_dfields[2, :Ni] = dW[:, 2]
+        D.append(O.assemble_K(cl, "polyharmonic", 2, 2, e, rows)[:Ni])
+
+    def adjoint(solve, solve_t):
+        c = solve(b)
+        u = A[:N] @ c
+        J = np.mean((u[:Ni] - ut[:Ni]) ** 2) + 1e-4 * np.sum(ctl ** 2)
+        dJdu = np.zeros(N)
+        dJdu[:Ni] = 2.0 * (u[:Ni] - ut[:Ni]) / Ni
+        lam = solve_t(A[:N].T @ dJdu)
+        dW = np.zeros((Ni, 5))
+        for kk in range(1, 5):
+            dW[:, kk] = -lam[:Ni] * (D[kk - 1] @ c)
+        dF = np.zeros((3, N))
+        dF[0, :Ni] = dW[:, 3] + dW[:, 4]
+        dF[1, :Ni] = dW[:, 1]
+        dF[2, :Ni] = dW[:, 2]
+        return J, lam[north] + 2e-4 * ctl, dF, u
+
+    # the plain LU of K, and the LU of K equilibrated by powers of two (rows, then columns, as the GPU path
+    # does): two backward-stable FP64 solves whose distance is this problem's FP64 floor
+    lu = sla.lu_factor(K)
+    J, dJ_dc, dJ_dfields, u = adjoint(lambda v: sla.lu_solve(lu, v), lambda v: sla.lu_solve(lu, v, trans=1))
+    r = 2.0 ** np.round(-np.log2(np.abs(K).max(1)))
+    cs = 2.0 ** np.round(-np.log2(np.abs(K * r[:, None]).max(0)))
+    lue = sla.lu_factor(K * r[:, None] * cs[None, :])
+    Je, dce, dFe, ue = adjoint(lambda v: cs * sla.lu_solve(lue, r * v), lambda v: r * sla.lu_solve(lue, cs * v, trans=1))
+    # and the plain LU of K with every entry moved by up to one unit in the last place (seeded): two FP64
+    # assemblies of the same matrix (closed forms evaluated in a different order) differ by that much
+    Kp = K * (1.0 + np.random.default_rng(2).uniform(-1.0, 1.0, K.shape) * 2.0 ** -53)
+    lup = sla.lu_factor(Kp)
+    Jp, dcp, dFp, up = adjoint(lambda v: sla.lu_solve(lup, v), lambda v: sla.lu_solve(lup, v, trans=1))
     np.savez_compressed(os.path.join(HERE, "full_control_100.npz"), control=ctl, J=np.array(J), dJ_dc=dJ_dc,
-                        dJ_dfields=dJ_dfields, vals=u)
-    print(f"control: J = {J:.6e}, {time.time() - t0:.1f} s", flush=True)
+                        dJ_dfields=dJ_dfields, vals=u, J_eq=np.array(Je), dJ_dc_eq=dce, dJ_dfields_eq=dFe,
+                        vals_eq=ue, J_ulp=np.array(Jp), dJ_dc_ulp=dcp, dJ_dfields_ulp=dFp, vals_ulp=up)
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    for name, (Jx, dcx, dFx, ux) in (("equilibrated LU", (Je, dce, dFe, ue)), ("entries moved by 1 ulp", (Jp, dcp, dFp, up))):
+        print(f"control: J = {J:.6e}; plain LU vs {name}: J {abs(J - Jx) / abs(J):.2e}, vals {rel(ux, u):.2e}, "
+              f"dJ/dc {rel(dcx, dJ_dc):.2e}, dJ/dfields {rel(dFx, dJ_dfields):.2e}", flush=True)
+    print(f"control: {time.time() - t0:.1f} s", flush=True)
 
 
 def advection():

@@ -50,7 +50,7 @@ def build(updes, case):
             self.nodes = {g: torch.tensor(coords[g]) for g in range(self.N)}
 
     cloud = InjectedCloud(Nx=case["Nx"], Ny=case["Ny"], facet_types=dict(case["facets"]),
-                          support_size="max")
+                          support_size=case.get("support", "max"))
     kind, param = case["rbf"]
     rbf = {"polyharmonic": lambda p: partial(updes.polyharmonic, a=int(p)),
            "gaussian": lambda p: partial(updes.gaussian, eps=p),
@@ -126,6 +126,8 @@ def run_case(updes, name, case):
         diffMat_rowsum=diffMat.sum(1), diffMat_rowabs=np.abs(diffMat).sum(1),
         A_rowsum=A.sum(1), A_rowabs=np.abs(A).sum(1),
     )
+    if case.get("support") is not None:
+        out["sorted_local_supports"] = np.asarray(npy(cloud.sorted_local_supports), dtype=np.int64)
     if diff_args is not None:
         out["fields"] = np.stack([npy(f) for f in diff_args])
     if rhs_args is not None:
@@ -143,10 +145,11 @@ def run_case(updes, name, case):
     print(f"{name}: N={N} n={N + M} {time.time() - t0:.1f}s")
 
 
-def run_adjoint(updes):
+def run_adjoint(updes, name=None):
     """Reverse-mode gradient through the reference solve (inv → GEMM → QR → inv)."""
     import jax.numpy as jnp
-    case = C.CASES[C.ADJOINT_CASE]
+    name = name or C.ADJOINT_CASE
+    case = C.CASES.get(name) or C.LOCAL_CASES[name]
     cloud, rbf, dop, rop, bcs, diff_args, rhs_args = build(updes, case)
     north = cloud.facet_nodes["North"]
     c0 = torch.tensor(C.adjoint_control(len(north)), requires_grad=True)
@@ -160,7 +163,8 @@ def run_adjoint(updes):
     Ni = cloud.Ni
     J = torch.mean((sol.vals[:Ni] - ut[:Ni]) ** 2) + C.ADJOINT_REG * torch.sum(c0 ** 2)
     J.backward()
-    np.savez_compressed(os.path.join(HERE, "adjoint_kgrad_10x10.npz"),
+    out_name = "adjoint_kgrad_10x10" if name == C.ADJOINT_CASE else f"adjoint_{name}"
+    np.savez_compressed(os.path.join(HERE, f"{out_name}.npz"),
                         control=c0.detach().numpy(), J=np.array(float(J)),
                         dJ_dc=c0.grad.numpy(), dJ_dfields=np.stack([f.grad.numpy() for f in fields]),
                         vals=sol.vals.detach().numpy())
@@ -298,7 +302,8 @@ if __name__ == "__main__":
         sys.exit("usage: make_golden.py <path of the Updes source tree> [case ...]")
     ref = sys.argv[1]
     updes = load_reference(ref)
-    only = sys.argv[2:] or list(C.CASES) + list(C.MULTI_CASES) + ["gmsh", "ref_fixture"]
+    only = sys.argv[2:] or (list(C.CASES) + list(C.MULTI_CASES) + list(C.LOCAL_CASES)
+                            + ["gmsh", "ref_fixture", "adjoint_local"])
     for name in only:
         if name == "adjoint":
             continue
@@ -308,8 +313,13 @@ if __name__ == "__main__":
         if name == "ref_fixture":
             run_ref_fixture(updes, ref)
             continue
+        if name == "adjoint_local":
+            run_adjoint(updes, C.LOCAL_ADJOINT_CASE)
+            continue
         if name in C.MULTI_CASES:
             run_multi(updes, name, C.MULTI_CASES[name])
+        elif name in C.LOCAL_CASES:
+            run_case(updes, name, C.LOCAL_CASES[name])
         else:
             run_case(updes, name, C.CASES[name])
     if len(sys.argv) <= 2 or "adjoint" in sys.argv[2:]:

@@ -42,8 +42,9 @@ def oracle_problem(case, compat=True):
     else:
         f_int = C.FUNCS[case["rhs"]](np, X[:Ni, 0], X[:Ni, 1])
     q = O.assemble_q(cloud, f_int, bcv)
+    supports = O.local_supports(X, case["support"]) if case.get("support") is not None else None
     return dict(cloud=cloud, rows=rows, W=W, q=q, kind=kind, param=param, deg=case["max_degree"],
-                fields=fields, robin=robin, bcv=bcv)
+                fields=fields, robin=robin, bcv=bcv, supports=supports)
 
 
 def case_of(g):

@@ -78,19 +78,32 @@ def _duplicate_node_system():
     return cloud, op, rhs, {f: (lambda c: 0.0 * c[0]) for f in facets}
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_duplicate_nodes_report_a_singular_system(precision):
-    """Two interior nodes at the same coordinates give two identical rows of K.  FP64 elimination turns the
-    second into exact zeros (LAPACK-style info > 0, UPDES_ERR_SINGULAR); the mixed path cannot refine on a
-    singular K and, after its FP64 fallback, ends the same way or reports that it did not converge."""
+def test_duplicate_nodes_are_rejected_on_the_host():
     cloud, op, rhs, bcs = _duplicate_node_system()
-    with pytest.raises(_lib.UpdesError) as ei:
-        U.pde_solver(op, rhs, cloud, bcs, U.polyharmonic, 1,
-                     options=U.SolverOptions(precision=precision, reuse_factorization=False))
-    assert ei.value.status in (_lib.ERR_SINGULAR, _lib.ERR_NOT_CONVERGED), str(ei.value)
-    if precision == "fp64":
-        assert ei.value.status == _lib.ERR_SINGULAR and U.LAST_INFO["lu_info"] > 0
-    # the context is still usable
+    with pytest.raises(ValueError, match="coincide"):
+        U.pde_solver(op, rhs, cloud, bcs, U.polyharmonic, 1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_duplicate_nodes_through_the_c_abi(precision):
+    """Two interior nodes at the same coordinates give two identical rows of K (condition number ~1e19).
+    Handed straight to updes_solve, the elimination meets a pivot at rounding level, not an exact zero (as
+    LAPACK's getrf does on the same matrix).  The call must come back with an error status, or with OK and
+    a finite backward error in its report (the FP64 path, like getrs, does not judge its answer; that is why
+    the host layer rejects such clouds), must not crash, and must leave the context usable."""
+    import torch
+    cloud, op, rhs, bcs = _duplicate_node_system()
+    o = U.SolverOptions(precision=precision, reuse_factorization=False)
+    W, kind, bnodes, geom, q = U.operators.prepare(op, rhs, U.SquareCloud(Nx=12, Ny=12, facet_types=dict(
+        cloud.facet_types)), bcs, U.polyharmonic, 1, options=o)
+    dp = U.operators.DeviceProblem(cloud, U.polyharmonic, 1, W, kind, bnodes, geom)
+    try:
+        _, _, info = U.operators.solve_device(dp, q, o)
+        print(precision, info)
+        assert np.isfinite(info["backward_error"]), info
+    except _lib.UpdesError as e:
+        assert e.status in (_lib.ERR_SINGULAR, _lib.ERR_NOT_CONVERGED), str(e)
+    torch.cuda.synchronize()
     sol = solve_case(C.CASES["poisson_jitter_11x11"], precision, reuse_factorization=False)[1]
     g = load("poisson_jitter_11x11")
     assert np.linalg.norm(sol.vals - g["vals"]) <= 1e-8 * np.linalg.norm(g["vals"])

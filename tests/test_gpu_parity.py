@@ -11,7 +11,7 @@ from oracle import updes_np as O
 from updes_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
-NAMES = list(C.CASES)
+NAMES = list(C.CASES) + list(C.LOCAL_CASES)
 
 
 def rel(a, b):
@@ -24,7 +24,7 @@ def test_assembly_matches_oracle(name, compat):
     """Every assembled entry within 1e-12 of the oracle, relative to its row's scale."""
     case = case_of(load(name))
     p = oracle_problem(case, compat=compat)
-    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"], supports=p["supports"])
     cl, dp, q = device_problem(case, compat=compat)
     K64, K32, ld = assemble(dp, fp32=True)
     Kg = K64.cpu().numpy()
@@ -65,7 +65,7 @@ def test_eval_kernels(name):
     vals = torch.empty(cl.N, dtype=torch.float64, device="cuda")
     _lib.check(lib.updes_eval_values(ctypes.byref(dp.c), c.data_ptr(), vals.data_ptr(), dp.stream()), "eval")
     p = oracle_problem(case)
-    want = O.eval_values(p["cloud"], p["kind"], p["param"], p["deg"], g["coeffs"])
+    want = O.eval_values(p["cloud"], p["kind"], p["param"], p["deg"], g["coeffs"], supports=p["supports"])
     assert rel(vals.cpu().numpy(), want) < 1e-12
     import updes_gb300 as U
     from gpu_helpers import rbf_callable
@@ -81,10 +81,15 @@ def test_eval_kernels(name):
 
 
 def _floor(g, p):
-    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
-    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"])
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"], supports=p["supports"])
+    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"], supports=p["supports"])
     u, c = O.solve_direct(K, A, p["q"])
-    return rel(u, g["vals"]), u
+    return rel(u, g["vals"]), u, K
+
+
+def _backward_error(K, c, q):
+    b = np.concatenate([q, np.zeros(K.shape[0] - q.shape[0])])
+    return np.abs(K @ c - b).max() / (np.abs(K) @ np.abs(c) + np.abs(b)).max()
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -96,12 +101,15 @@ def test_solve_matches_reference(name, precision):
     g = load(name)
     case = case_of(g)
     p = oracle_problem(case)
-    floor, u_or = _floor(g, p)
+    floor, u_or, K = _floor(g, p)
     cl, sol = solve_case(case, precision)
     tol = (1e-10 if precision == "fp64" else 1e-8)
     err = rel(sol.vals, g["vals"])
     assert err <= max(tol, 3 * floor), (err, floor, U.LAST_INFO)
     assert rel(sol.vals, u_or) <= max(tol, 3 * floor)
+    # coefficients: as backward-stable as the reference's own on the oracle's K (coefficients of these
+    # ill-conditioned systems are far less determined than vals, so they are compared through the residual)
+    assert _backward_error(K, sol.coeffs, p["q"]) <= max(1e-13, 10 * _backward_error(K, g["coeffs"], p["q"]))
     assert U.LAST_INFO["converged"] == 1
     if precision == "fp32":
         assert U.LAST_INFO["fell_back"] == 0, U.LAST_INFO
@@ -118,7 +126,7 @@ def test_mat_materialises_reference_B():
 
 # Double-float assembly: every polyharmonic golden case, plus polyharmonic variants of the periodic and the
 # Robin (Gaussian) cases so that every row kind is covered (r^3 and r^5).
-DF_CASES = [nm for nm in NAMES if C.CASES[nm]["rbf"][0] == "polyharmonic"] + [
+DF_CASES = [nm for nm in C.CASES if C.CASES[nm]["rbf"][0] == "polyharmonic"] + [
     "periodic_imq_8x7@1", "gaussian_dnr_9x8@2", "thinplate_deg4_8x8@1"]
 
 
@@ -361,3 +369,35 @@ def test_factor_once_solve_many():
     assert U.LAST_INFO["reused_factors"]
     assert rel(s2.vals, s1.vals) < 1e-12
     assert rel(s1.vals, g["vals"]) < 1e-8
+
+
+@pytest.mark.parametrize("name", list(C.LOCAL_CASES))
+def test_local_support_mat_and_coefficients(name):
+    """Local supports through the rest of the solve's outputs: the materialised B against the reference's,
+    core_compute_coefficients (A with local supports) against the oracle, and the batched evaluation, which
+    does not take local supports, refusing them."""
+    import torch
+
+    import updes_gb300 as U
+    from gpu_helpers import rbf_callable
+    g = load(name)
+    case = case_of(g)
+    p = oracle_problem(case)
+    cl, sol = solve_case(case, "fp64")
+    assert rel(sol.mat.materialize(), g["B"]) < 1e-8
+    f = np.sin(3 * cl.sorted_nodes[:, 0]) + cl.sorted_nodes[:, 1]
+    got = U.compute_coefficients(f, cl, rbf_callable(case), case["max_degree"])
+    want = O.field_coefficients(p["cloud"], p["kind"], p["param"], p["deg"], f, supports=p["supports"])
+    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"], supports=p["supports"])
+    assert np.abs(A @ got - np.concatenate([f, np.zeros(dp_M(case))])).max() <= 1e-12 * np.abs(A).max() * max(
+        np.abs(got).max(), 1.0)
+    assert rel(A[:cl.N] @ got, A[:cl.N] @ want) < 1e-10
+    _, dp, _ = device_problem(case)
+    C_ = torch.zeros((dp.n, 2), dtype=torch.float64, device="cuda")
+    V = torch.zeros((dp.N, 2), dtype=torch.float64, device="cuda")
+    st = _lib.load().updes_eval_values_batch(ctypes.byref(dp.c), 2, C_.data_ptr(), 2, V.data_ptr(), 2, dp.stream())
+    assert st == _lib.ERR_UNSUPPORTED
+
+
+def dp_M(case):
+    return O.nb_monomials(case["max_degree"])

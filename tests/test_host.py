@@ -19,7 +19,7 @@ NAMES = list(C.CASES)
 
 def product_cloud(case):
     return U.SquareCloud(Nx=case["Nx"], Ny=case["Ny"], facet_types=dict(case["facets"]),
-                         coords=C.grid_coords(case))
+                         coords=C.grid_coords(case), support_size=case.get("support", "max"))
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -173,3 +173,26 @@ def test_invalid_arguments_rejected_without_gpu():
     assert lib.updes_lu_workspace(0, 0, ctypes.byref(nb)) == _lib.ERR_INVALID
     assert lib.updes_lu_workspace(100, 5, ctypes.byref(nb)) == _lib.ERR_INVALID
     assert lib.updes_lu_workspace(100, 1, ctypes.byref(nb)) == _lib.OK and nb.value > 0
+
+
+@pytest.mark.parametrize("name", list(C.LOCAL_CASES))
+def test_local_supports_match_reference(name):
+    """SquareCloud(support_size=k): every node's support, as a set, equals the reference's BallTree result;
+    GmshCloud takes the same path (updes/cloud.py:83-112)."""
+    g = load(name)
+    cl = product_cloud(case_of(g))
+    ref = g["sorted_local_supports"]
+    assert cl.sorted_local_supports.shape == ref.shape and cl.sorted_local_supports.dtype == np.int32
+    assert all(set(a) == set(b) for a, b in zip(cl.sorted_local_supports.tolist(), ref.tolist()))
+
+
+def test_support_size_edge_values():
+    facets = {"South": "d", "West": "d", "North": "d", "East": "d"}
+    assert U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size=20).sorted_local_supports is None
+    assert U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size="max").sorted_local_supports is None
+    with pytest.raises(AssertionError):
+        U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size=21)
+    with pytest.raises(ValueError):
+        U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size=1)
+    with pytest.raises(ValueError):
+        U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size=2.5)

@@ -8,7 +8,7 @@ import cases as C
 from golden_problem import case_of, load, oracle_problem
 from oracle import updes_np as O
 
-NAMES = list(C.CASES)
+NAMES = list(C.CASES) + list(C.LOCAL_CASES)
 
 
 def rel(a, b):
@@ -33,8 +33,9 @@ def test_assembly_entries(name):
     """Assembled entries agree with the reference within 1e-12 (relative to the row scale)."""
     g = load(name)
     p = oracle_problem(case_of(g))
-    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
-    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"])
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"],
+                     supports=p["supports"])
+    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"], supports=p["supports"])
     N = p["cloud"].N
     D = K[:N]
     if "diffMat" in g:
@@ -66,8 +67,9 @@ def test_solution_faithful(name):
     """The oracle's restatement of the reference's solve order reproduces vals and coeffs."""
     g = load(name)
     p = oracle_problem(case_of(g))
-    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
-    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"])
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"],
+                     supports=p["supports"])
+    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"], supports=p["supports"])
     u, c, B = O.solve_faithful(K, A, p["q"])
     assert rel(u, g["vals"]) < 1e-9
     if "B" in g:
@@ -79,8 +81,9 @@ def test_solution_direct(name):
     """One LU of the Kansa matrix gives the reference's solution (formulation check)."""
     g = load(name)
     p = oracle_problem(case_of(g))
-    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"])
-    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"])
+    K = O.assemble_K(p["cloud"], p["kind"], p["param"], p["deg"], p["W"], p["rows"],
+                     supports=p["supports"])
+    A = O.assemble_A(p["cloud"], p["kind"], p["param"], p["deg"], supports=p["supports"])
     u, c = O.solve_direct(K, A, p["q"])
     assert rel(u, g["vals"]) < 1e-8
 
@@ -94,3 +97,13 @@ def test_field_operators(name):
     gr = O.gradient(X, g["coeffs"], X, p["kind"], p["param"])
     assert rel(v, g["value_at_nodes"]) < 1e-12
     assert rel(gr, g["grad_at_nodes"]) < 1e-12
+
+
+@pytest.mark.parametrize("name", list(C.LOCAL_CASES))
+def test_local_supports_match_the_reference(name):
+    """The k - 1 nearest other nodes of every node, as sets, equal the reference's BallTree supports."""
+    g = load(name)
+    p = oracle_problem(case_of(g))
+    ref = g["sorted_local_supports"]
+    assert p["supports"].shape == ref.shape
+    assert all(set(a) == set(b) for a, b in zip(p["supports"].tolist(), ref.tolist()))

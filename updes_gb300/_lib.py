@@ -41,9 +41,9 @@ class UpdesError(RuntimeError):
 class Problem(ctypes.Structure):
     _fields_ = [
         ("N", ctypes.c_int32), ("Ni", ctypes.c_int32), ("M", ctypes.c_int32), ("rbf", ctypes.c_int32),
-        ("rbf_param", ctypes.c_double), ("self_term", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("rbf_param", ctypes.c_double), ("self_term", ctypes.c_int32), ("support_width", ctypes.c_int32),
         ("nodes", ctypes.c_void_p), ("op_weights", ctypes.c_void_p), ("bd_kind", ctypes.c_void_p),
-        ("bd_node", ctypes.c_void_p), ("bd_geom", ctypes.c_void_p),
+        ("bd_node", ctypes.c_void_p), ("bd_geom", ctypes.c_void_p), ("supports", ctypes.c_void_p),
     ]
 
 

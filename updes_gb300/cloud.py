@@ -4,7 +4,12 @@
 normals) and the renumbering of updes/cloud.py:115-172 (internal, Dirichlet,
 Neumann, Robin, periodic), vectorised.  With support_size="max" every node's
 support is "all other nodes" (updes/cloud.py:97-112), so the N x (N-1)
-support table is never materialised.
+support table is never materialised.  With an integer support_size every
+node's support is its support_size - 1 nearest other nodes
+(``sorted_local_supports``, updes/cloud.py:83-112), found with SciPy's
+KD-tree instead of the reference's BallTree: the same sets wherever no two
+candidates are equally far at the edge of a support (the order inside a
+support does not matter to any matrix built from it).
 """
 from __future__ import annotations
 
@@ -15,9 +20,12 @@ class Cloud:
     """Common attributes of a meshfree cloud (updes/cloud.py:10-49)."""
 
     def __init__(self, facet_types, support_size="max"):
-        if support_size not in ("max", None):
-            raise NotImplementedError("only support_size='max' (global collocation) is implemented")
-        self.support_size = "max"
+        if support_size is None:
+            support_size = "max"
+        if support_size != "max" and (isinstance(support_size, bool) or not isinstance(support_size, (int, np.integer))):
+            raise ValueError(f"support_size must be 'max' or an int, not {support_size!r}")
+        self.support_size = support_size if support_size == "max" else int(support_size)
+        self.sorted_local_supports = None
         self.dim = 2
         self.N = self.Ni = self.Nd = self.Nn = self.Nr = 0
         self.Np = []
@@ -98,10 +106,27 @@ class SquareCloud(Cloud):
         self.has_normal[new[has]] = True
         self.outward_normals = {int(i): self.normals_by_node[i] for i in np.flatnonzero(self.has_normal)}
         self.sorted_outward_normals = self.normals_by_node[self.has_normal]
+        self.sorted_local_supports = _define_local_supports(self)
 
     @property
     def nodes(self):
         return {i: self.sorted_nodes[i] for i in range(self.N)}
+
+
+def _define_local_supports(cloud):
+    """(N, support_size - 1) int32 supports in sorted node order, or None for "max" (updes/cloud.py:83-112:
+    the support_size nearest nodes of each node, the first of them, the node itself, dropped)."""
+    k = cloud.support_size
+    if k == "max" or k == cloud.N:  # every other node (support_size = N is the same as "max")
+        return None
+    if not 0 < k <= cloud.N:
+        raise AssertionError("Support size must be strictly greater than 0 and at most the number of nodes")
+    if k == 1:
+        raise ValueError("support_size 1 leaves every support empty: the collocation matrix would be singular")
+    from scipy.spatial import cKDTree
+    _, nb = cKDTree(cloud.sorted_nodes).query(cloud.sorted_nodes, k=k)
+    nb = np.asarray(nb, dtype=np.int64).reshape(cloud.N, k)
+    return np.ascontiguousarray(nb[:, 1:], dtype=np.int32)
 
 
 class GmshCloud(Cloud):
@@ -135,6 +160,7 @@ class GmshCloud(Cloud):
         self._read()
         self._normals()
         self._renumber()
+        self.sorted_local_supports = _define_local_supports(self)
 
     @staticmethod
     def _meshfile(filename, mesh_save_location):

@@ -5,6 +5,7 @@
 // evaluates vals = [Phi P] c (updes/assembly.py:404-410 read backwards).
 #include "common.cuh"
 #include "df.cuh"
+#include "entries.cuh"
 #include "rbf.cuh"
 #include "stats.cuh"
 
@@ -14,106 +15,6 @@ constexpr int kAsmRowsPerWarp = 8;
 constexpr int kAsmWarps = 8;
 constexpr int kAsmRows = kAsmRowsPerWarp * kAsmWarps;  // 64 rows per CTA
 constexpr int kAsmCols = 128;                          // 32 lanes x 4 columns
-
-struct RowInfo {
-  int kind;  // -1 interior, -2 P^T row, else UPDES_ROW_*
-  int a, b;  // evaluation node, partner node
-  double xa, ya, xb, yb;
-  double w0, w1, w2, w3, w4;  // interior: value, d/dx, d/dy, d2/dx2, d2/dy2
-  double n1x, n1y, n2x, n2y, nPx, nPy, beta;
-};
-
-__device__ __forceinline__ RowInfo load_row(const updes_problem& p, int r) {
-  RowInfo ri;
-  if (r < p.Ni) {
-    ri.kind = -1;
-    ri.a = ri.b = r;
-    const double* w = p.op_weights + 5ll * r;
-    ri.w0 = w[0]; ri.w1 = w[1]; ri.w2 = w[2]; ri.w3 = w[3]; ri.w4 = w[4];
-    ri.n1x = ri.n1y = ri.n2x = ri.n2y = ri.nPx = ri.nPy = ri.beta = 0.0;
-  } else if (r < p.N) {
-    const int b = r - p.Ni;
-    ri.kind = p.bd_kind[b];
-    ri.a = p.bd_node[2 * b];
-    ri.b = p.bd_node[2 * b + 1];
-    const double* g = p.bd_geom + 8ll * b;
-    ri.n1x = g[0]; ri.n1y = g[1]; ri.n2x = g[2]; ri.n2y = g[3];
-    ri.nPx = g[4]; ri.nPy = g[5]; ri.beta = g[6];
-    ri.w0 = ri.w1 = ri.w2 = ri.w3 = ri.w4 = 0.0;
-  } else {
-    ri.kind = -2;
-    ri.a = ri.b = r - p.N;  // monomial id
-    ri.w0 = ri.w1 = ri.w2 = ri.w3 = ri.w4 = 0.0;
-    ri.n1x = ri.n1y = ri.n2x = ri.n2y = ri.nPx = ri.nPy = ri.beta = 0.0;
-    ri.xa = ri.ya = ri.xb = ri.yb = 0.0;
-    return ri;
-  }
-  ri.xa = p.nodes[2ll * ri.a];
-  ri.ya = p.nodes[2ll * ri.a + 1];
-  ri.xb = p.nodes[2ll * ri.b];
-  ri.yb = p.nodes[2ll * ri.b + 1];
-  return ri;
-}
-
-// Entry (row, node column c) of K for c < N.
-template <int KIND>
-__device__ __forceinline__ double entry_rbf(const RowInfo& ri, int c, double xc, double yc, double param,
-                                            int ip, int self_term) {
-  if (ri.kind == -2) {  // P^T row: monomial(ri.a) at node c
-    const MonoT m = monomial_terms(ri.a, xc, yc);
-    return m.m;
-  }
-  const double dx = ri.xa - xc, dy = ri.ya - yc;
-  const double r2 = dx * dx + dy * dy;
-  if (ri.kind == -1) {
-    if (c == ri.a && !self_term) return 0.0;
-    if (r2 == 0.0) return ri.w0 * rbf_phi0<KIND>();
-    const RbfG g = rbf_g<KIND>(r2, param, ip);
-    return ri.w0 * g.phi + g.g1 * (ri.w1 * dx + ri.w2 * dy + (ri.w3 + ri.w4)) +
-           g.g2 * (ri.w3 * dx * dx + ri.w4 * dy * dy);
-  }
-  if (ri.kind <= UPDES_ROW_ROBIN) {
-    if (c == ri.a && !self_term) return 0.0;
-    if (r2 == 0.0) return (ri.kind == UPDES_ROW_NEUMANN) ? 0.0 : (ri.kind == UPDES_ROW_ROBIN ? ri.beta : 1.0) * rbf_phi0<KIND>();
-    const RbfG g = rbf_g<KIND>(r2, param, ip);
-    if (ri.kind == UPDES_ROW_DIRICHLET) return g.phi;
-    const double fl = g.g1 * (ri.n1x * dx + ri.n1y * dy);
-    if (ri.kind == UPDES_ROW_NEUMANN) return fl;
-    return ri.beta * g.phi + fl;
-  }
-  // periodic rows span every column
-  const double ex = ri.xb - xc, ey = ri.yb - yc;
-  const double s2 = ex * ex + ey * ey;
-  RbfG ga, gb;
-  if (r2 == 0.0) { ga.phi = rbf_phi0<KIND>(); ga.g1 = 0.0; ga.g2 = 0.0; } else ga = rbf_g<KIND>(r2, param, ip);
-  if (s2 == 0.0) { gb.phi = rbf_phi0<KIND>(); gb.g1 = 0.0; gb.g2 = 0.0; } else gb = rbf_g<KIND>(s2, param, ip);
-  if (ri.kind == UPDES_ROW_PERIODIC_VALUE) return ga.phi - gb.phi;
-  return ga.g1 * (ri.n1x * dx + ri.n1y * dy) + gb.g1 * (ri.n2x * ex + ri.n2y * ey);
-}
-
-// Entry (row, monomial column k) of K.
-__device__ __forceinline__ double entry_mono(const RowInfo& ri, int k) {
-  if (ri.kind == -2) return 0.0;
-  const MonoT m = monomial_terms(k, ri.xa, ri.ya);
-  switch (ri.kind) {
-    case -1:
-      return ri.w0 * m.m + ri.w1 * m.mx + ri.w2 * m.my + ri.w3 * m.mxx + ri.w4 * m.myy;
-    case UPDES_ROW_DIRICHLET:
-      return m.m;
-    case UPDES_ROW_NEUMANN:
-      return m.mx * ri.nPx + m.my * ri.nPy;
-    case UPDES_ROW_ROBIN:
-      return ri.beta * m.m + (m.mx * ri.nPx + m.my * ri.nPy);
-    case UPDES_ROW_PERIODIC_VALUE: {
-      const MonoT q = monomial_terms(k, ri.xb, ri.yb);
-      return m.m - q.m;
-    }
-    default: {
-      const MonoT q = monomial_terms(k, ri.xb, ri.yb);
-      return (m.mx * ri.n1x + m.my * ri.n1y) + (q.mx * ri.n2x + q.my * ri.n2y);
-    }
-  }
-}
 
 template <int KIND>
 __global__ void __launch_bounds__(256) assemble_kernel(updes_problem p, int n, double* __restrict__ K64,
@@ -136,6 +37,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(updes_problem p, int n, d
     }
   }
   const int rbase = blockIdx.y * kAsmRows + warp * kAsmRowsPerWarp;
+  const bool local = p.supports != nullptr;  // local supports: assemble_local_kernel writes the Phi columns
   for (int i = 0; i < kAsmRowsPerWarp; ++i) {
     const int r = rbase + i;
     if (r >= n) break;
@@ -144,7 +46,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(updes_problem p, int n, d
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int64_t c = c0 + u;
-      if (c < p.N) v[u] = entry_rbf<KIND>(ri, int(c), xc[u], yc[u], param, ip, p.self_term);
+      if (c < p.N) v[u] = (local && ri.kind != -2) ? 0.0 : entry_rbf<KIND>(ri, int(c), xc[u], yc[u], param, ip, p.self_term);
       else if (c < n) v[u] = entry_mono(ri, int(c - p.N));
       else v[u] = 0.0;
     }
@@ -167,6 +69,113 @@ __global__ void __launch_bounds__(256) assemble_kernel(updes_problem p, int n, d
     }
   }
 }
+
+// Local supports (p.supports, p.support_width = S): the Phi columns of row r < N are the support of its node
+// (updes/assembly.py:20-32, 125-128, 169-212), of both its nodes on a periodic row (assembly.py:215-258).
+// assemble_kernel has written zeros there; one warp per row writes the support's entries.  A column in both
+// supports of a periodic row is written twice with the same value.
+template <int KIND>
+__global__ void __launch_bounds__(256) assemble_local_kernel(updes_problem p, double* __restrict__ K64, int64_t ld64,
+                                                             float* __restrict__ K32, int64_t ld32) {
+  const int r = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= p.N) return;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const RowInfo ri = load_row(p, r);
+  const int S = p.support_width;
+  const bool two = ri.kind == UPDES_ROW_PERIODIC_VALUE || ri.kind == UPDES_ROW_PERIODIC_FLUX;
+  for (int t = lane; t < (two ? 2 * S : S); t += 32) {
+    const int node = t < S ? ri.a : ri.b;
+    const int c = p.supports[int64_t(node) * S + (t < S ? t : t - S)];
+    const double v = entry_rbf<KIND>(ri, c, p.nodes[2ll * c], p.nodes[2ll * c + 1], p.rbf_param, ip, p.self_term);
+    if (K64) K64[int64_t(r) * ld64 + c] = v;
+    if (K32) K32[int64_t(r) * ld32 + c] = float(v);
+  }
+}
+
+// vals[i] = sum_{j in S(i)} phi(x_i - x_j) c_j + sum_k m_k(x_i) c_{N+k} with local supports (one warp per row).
+template <int KIND>
+__global__ void __launch_bounds__(256) eval_values_local_kernel(updes_problem p, const double* __restrict__ coeffs,
+                                                                double* __restrict__ vals) {
+  const int r = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= p.N) return;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int S = p.support_width;
+  const double xi = p.nodes[2ll * r], yi = p.nodes[2ll * r + 1];
+  double acc = 0.0;
+  for (int t = lane; t < S; t += 32) {
+    const int c = p.supports[int64_t(r) * S + t];
+    acc += rbf_value<KIND>(xi - p.nodes[2ll * c], yi - p.nodes[2ll * c + 1], p.rbf_param, ip) * coeffs[c];
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    for (int k = 0; k < p.M; ++k) acc += monomial_terms(k, xi, yi).m * coeffs[p.N + k];
+    vals[r] = acc;
+  }
+}
+
+// out[j] += sum over rows i whose support holds j of phi(x_i - x_j) g_i (the Phi^T g part of [Phi P]^T g with
+// local supports, where Phi is not symmetric): one warp per row, FP64 atomic adds into a zeroed out[0, N),
+// so the summation order, and the last bits, can differ between calls.
+template <int KIND>
+__global__ void __launch_bounds__(256) eval_values_local_t_kernel(updes_problem p, const double* __restrict__ g,
+                                                                  double* __restrict__ out) {
+  const int r = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= p.N) return;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int S = p.support_width;
+  const double xi = p.nodes[2ll * r], yi = p.nodes[2ll * r + 1], gi = g[r];
+  for (int t = lane; t < S; t += 32) {
+    const int c = p.supports[int64_t(r) * S + t];
+    atomicAdd(out + c, rbf_value<KIND>(xi - p.nodes[2ll * c], yi - p.nodes[2ll * c + 1], p.rbf_param, ip) * gi);
+  }
+}
+
+// coeff_grad_kernel with local supports: dW[i][k] = -lambda_i (sum_{j in S(i)} D_k(x_i, x_j) c_j + monomials).
+template <int KIND>
+__global__ void __launch_bounds__(256) coeff_grad_local_kernel(updes_problem p, const double* __restrict__ coeffs,
+                                                               const double* __restrict__ lambda,
+                                                               double* __restrict__ dW) {
+  const int r = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= p.Ni) return;
+  const int ip = (KIND == UPDES_RBF_POLYHARMONIC) ? 2 * int(p.rbf_param) + 1 : int(p.rbf_param);
+  const int S = p.support_width;
+  const double xi = p.nodes[2ll * r], yi = p.nodes[2ll * r + 1];
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int t = lane; t < S; t += 32) {
+    const int c = p.supports[int64_t(r) * S + t];
+    const double dx = xi - p.nodes[2ll * c], dy = yi - p.nodes[2ll * c + 1];
+    const double r2 = dx * dx + dy * dy, cj = coeffs[c];
+    if (r2 == 0.0) { acc[0] += rbf_phi0<KIND>() * cj; continue; }
+    const RbfG gg = rbf_g<KIND>(r2, p.rbf_param, ip);
+    acc[0] += gg.phi * cj;
+    acc[1] += gg.g1 * dx * cj;
+    acc[2] += gg.g1 * dy * cj;
+    acc[3] += (gg.g1 + gg.g2 * dx * dx) * cj;
+    acc[4] += (gg.g1 + gg.g2 * dy * dy) * cj;
+  }
+  for (int k = 0; k < 5; ++k)
+    for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+  if (lane == 0) {
+    for (int m = 0; m < p.M; ++m) {
+      const MonoT mt = monomial_terms(m, xi, yi);
+      const double gm = coeffs[p.N + m];
+      acc[0] += mt.m * gm; acc[1] += mt.mx * gm; acc[2] += mt.my * gm; acc[3] += mt.mxx * gm; acc[4] += mt.myy * gm;
+    }
+    const double l = lambda[r];
+    for (int k = 0; k < 5; ++k) dW[5ll * r + k] = -l * acc[k];
+  }
+}
+
+// Launch KERNEL<KIND> for the problem's kernel kind with the given grid and arguments.
+#define UPDES_DISPATCH_KIND(KERNEL, GRID, BLOCK, STREAM, ...)                                                        \
+  switch (p->rbf) {                                                                                               \
+    case UPDES_RBF_POLYHARMONIC: KERNEL<UPDES_RBF_POLYHARMONIC><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;   \
+    case UPDES_RBF_GAUSSIAN: KERNEL<UPDES_RBF_GAUSSIAN><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;           \
+    case UPDES_RBF_MULTIQUADRIC: KERNEL<UPDES_RBF_MULTIQUADRIC><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;   \
+    case UPDES_RBF_INVERSE_MULTIQUADRIC:                                                                          \
+      KERNEL<UPDES_RBF_INVERSE_MULTIQUADRIC><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;                     \
+    default: KERNEL<UPDES_RBF_THIN_PLATE><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;                          \
+  }
 
 // vals[i] = sum_{j != i} phi(x_i - x_j) c_j + sum_k m_k(x_i) c_{N+k}
 constexpr int kEvalRows = 16;     // rows per CTA (2 per warp)
@@ -719,6 +728,8 @@ int check_problem(const updes_problem* p) {
   if (!p->nodes) return UPDES_ERR_INVALID;
   if (p->Ni > 0 && !p->op_weights) return UPDES_ERR_INVALID;
   if (p->N > p->Ni && (!p->bd_kind || !p->bd_node || !p->bd_geom)) return UPDES_ERR_INVALID;
+  if (p->support_width < 0 || p->support_width >= p->N || (p->support_width > 0) != (p->supports != nullptr))
+    return UPDES_ERR_INVALID;
   return UPDES_OK;
 }
 
@@ -753,6 +764,11 @@ extern "C" int updes_assemble(const updes_problem* p, double* K64, int64_t ld64,
       assemble_kernel<UPDES_RBF_THIN_PLATE><<<grid, block, 0, s>>>(*p, n, K64, ld64, K32, ld32, ncols); break;
   }
   UPDES_LAUNCH_CHECK();
+  if (p->supports) {
+    const unsigned g = unsigned(ceil_div(int64_t(p->N) * 32, 256));
+    UPDES_DISPATCH_KIND(assemble_local_kernel, g, 256, s, *p, K64, ld64, K32, ld32);
+    UPDES_LAUNCH_CHECK();
+  }
   return UPDES_OK;
 }
 
@@ -766,7 +782,7 @@ extern "C" int updes_assemble_df(const updes_problem* p, float* Khi, float* Klo,
                                  int32_t* range_flag, void* scratch, size_t scratch_bytes, void* stream) {
   int st = check_problem(p);
   if (st) return st;
-  if (p->rbf != UPDES_RBF_POLYHARMONIC) return UPDES_ERR_UNSUPPORTED;
+  if (p->rbf != UPDES_RBF_POLYHARMONIC || p->supports) return UPDES_ERR_UNSUPPORTED;
   const int n = p->N + p->M;
   if (!Khi || !Klo || ld < n || ld % 4 || !scratch) return UPDES_ERR_INVALID;
   if (((reinterpret_cast<uintptr_t>(Khi) | reinterpret_cast<uintptr_t>(Klo) | reinterpret_cast<uintptr_t>(scratch)) &
@@ -877,6 +893,12 @@ int eval_values_sym(const updes_problem* p, const double* coeffs, double* vals, 
   int st = check_problem(p);
   if (st) return st;
   if (!coeffs || !vals || !part) return UPDES_ERR_INVALID;
+  if (p->supports) {  // local supports: Phi is sparse and not symmetric
+    UPDES_DISPATCH_KIND(eval_values_local_kernel, unsigned(ceil_div(int64_t(p->N) * 32, 256)), 256, s, *p, coeffs,
+                        vals);
+    UPDES_LAUNCH_CHECK();
+    return UPDES_OK;
+  }
   const int nblk = int(ceil_div(p->N, kSymT));
   const dim3 grid{unsigned(nblk), unsigned(nblk)};
   if (df && p->rbf == UPDES_RBF_POLYHARMONIC) {
@@ -907,6 +929,12 @@ extern "C" int updes_eval_values(const updes_problem* p, const double* coeffs, d
   if (st) return st;
   if (!coeffs || !vals) return UPDES_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->supports) {
+    UPDES_DISPATCH_KIND(eval_values_local_kernel, unsigned(ceil_div(int64_t(p->N) * 32, 256)), 256, s, *p, coeffs,
+                        vals);
+    UPDES_LAUNCH_CHECK();
+    return UPDES_OK;
+  }
   const unsigned grid = unsigned(ceil_div(p->N, kEvalRows));
   switch (p->rbf) {
     case UPDES_RBF_POLYHARMONIC: eval_values_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, coeffs, vals); break;
@@ -945,6 +973,12 @@ extern "C" int updes_coeff_grad(const updes_problem* p, const double* coeffs, co
   if (!coeffs || !lambda || !dW) return UPDES_ERR_INVALID;
   if (p->Ni == 0) return UPDES_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->supports) {
+    UPDES_DISPATCH_KIND(coeff_grad_local_kernel, unsigned(ceil_div(int64_t(p->Ni) * 32, 256)), 256, s, *p, coeffs,
+                        lambda, dW);
+    UPDES_LAUNCH_CHECK();
+    return UPDES_OK;
+  }
   const unsigned grid = unsigned(ceil_div(p->Ni, kEvalRows));
   switch (p->rbf) {
     case UPDES_RBF_POLYHARMONIC: coeff_grad_kernel<UPDES_RBF_POLYHARMONIC><<<grid, 256, 0, s>>>(*p, coeffs, lambda, dW); break;
@@ -962,6 +996,14 @@ extern "C" int updes_eval_values_t(const updes_problem* p, const double* g, doub
   if (st) return st;
   if (!g || !out) return UPDES_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->supports) {
+    UPDES_CUDA_TRY(cudaMemsetAsync(out, 0, size_t(p->N) * sizeof(double), s));
+    UPDES_DISPATCH_KIND(eval_values_local_t_kernel, unsigned(ceil_div(int64_t(p->N) * 32, 256)), 256, s, *p, g, out);
+    UPDES_LAUNCH_CHECK();
+    pt_matvec_kernel<<<1, 1024, 0, s>>>(*p, g, out);
+    UPDES_LAUNCH_CHECK();
+    return UPDES_OK;
+  }
   const unsigned grid = unsigned(ceil_div(p->N, kEvalRows));
   // Phi is symmetric (radial kernel, same zero diagonal), so Phi^T g = Phi g
   switch (p->rbf) {
@@ -982,6 +1024,7 @@ extern "C" int updes_eval_values_batch(const updes_problem* p, int32_t R, const 
   int st = check_problem(p);
   if (st) return st;
   if (!C || !vals || R <= 0 || R > 64 || ldc < R || ldv < R) return UPDES_ERR_INVALID;
+  if (p->supports) return UPDES_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const unsigned grid = unsigned(ceil_div(p->N, kEvBRows));
   switch (p->rbf) {

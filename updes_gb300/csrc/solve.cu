@@ -496,9 +496,11 @@ int read_status(DeviceStatus* st, cudaStream_t s, DeviceStatus* host) {
 }
 
 // hi = float(v), lo = float(v - hi) with v = dr_i K_ij dc_j (scalings exact; dr, dc may be null)
-__global__ void split_df_kernel(const double* __restrict__ K, int64_t ldk, float* __restrict__ hi,
+// hi/lo planes of the scaled K (none when hi is null); with write_back the scaled FP64 entry also replaces
+// K's (each thread reads and writes only its own entry, so K may be read and written in place; ldk == ld then).
+__global__ void split_df_kernel(double* __restrict__ K, int64_t ldk, float* __restrict__ hi,
                                 float* __restrict__ lo, int64_t ld, int n, const double* __restrict__ dr,
-                                const double* __restrict__ dc) {
+                                const double* __restrict__ dc, int write_back) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t i = e / ld, j = e % ld;
   if (i >= n) return;
@@ -508,9 +510,12 @@ __global__ void split_df_kernel(const double* __restrict__ K, int64_t ldk, float
     if (dr) v *= dr[i];
     if (dc) v *= dc[j];
   }
-  const float h = float(v);
-  hi[i * ld + j] = h;
-  lo[i * ld + j] = float(v - double(h));
+  if (hi) {
+    const float h = float(v);
+    hi[i * ld + j] = h;
+    lo[i * ld + j] = float(v - double(h));
+  }
+  if (write_back) K[i * ldk + j] = v;
 }
 
 int perm_core(int n, int32_t* piv, cudaStream_t s) {
@@ -535,7 +540,7 @@ int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t l
   if (precision == UPDES_PREC_FP32) {
     if (!w.lo || !F) return UPDES_ERR_INVALID;
     split_df_kernel<<<unsigned(ceil_div(int64_t(n) * ldf, 256)), 256, 0, s>>>(A, lda, static_cast<float*>(F), w.lo,
-                                                                              ldf, n, nullptr, nullptr);
+                                                                              ldf, n, nullptr, nullptr, 0);
     UPDES_LAUNCH_CHECK();
     return factor_df_core(n, static_cast<float*>(F), w.lo, ldf, piv, w, s);
   }
@@ -954,7 +959,8 @@ extern "C" int updes_solve_workspace(const updes_problem* p, const updes_solve_o
 namespace {
 
 // Factors of the equilibrated K (double-float planes) at `precision`; records the factored state.
-// planes_ready: the working planes (F32, Wlo) already hold the equilibrated K (written by the assembly).
+// planes_ready: the working copy already holds the equilibrated K, written by the assembly: for FP32 factors
+// the planes F32 and Wlo (double-float assembly), for FP64 factors the FP64 matrix W.
 int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info, cudaStream_t s,
                  bool planes_ready = false) {
   Timer t(s);
@@ -962,8 +968,10 @@ int factor_stage(const SolveWs& w, int n, int precision, updes_solve_info* info,
   UPDES_CUDA_TRY(cudaMemsetAsync(w.state, 0, 4 * sizeof(int32_t), s));  // invalid until the factors are complete
   const int64_t total = int64_t(n) * w.ld;
   if (precision == UPDES_PREC_FP64) {
-    join_df_kernel<<<unsigned(ceil_div(total, 256)), 256, 0, s>>>(w.Khi, w.Klo, w.W, total);
-    UPDES_LAUNCH_CHECK();
+    if (!planes_ready) {  // a fallback after the FP32 attempt: W was overwritten, K is rebuilt from its planes
+      join_df_kernel<<<unsigned(ceil_div(total, 256)), 256, 0, s>>>(w.Khi, w.Klo, w.W, total);
+      UPDES_LAUNCH_CHECK();
+    }
     e = factor_core(n, w.W, w.ld, precision, nullptr, w.ld, w.piv, w.lu, s);
   } else {
     if (!planes_ready) {
@@ -1033,7 +1041,8 @@ int assemble_df_stage(const updes_problem* p, const SolveWs& w, int n, cudaStrea
 
 // Assemble K and its power-of-two equilibration into the double-float planes: in double-float arithmetic for
 // a polyharmonic system factored in FP32, else in FP64.
-// *planes_ready: the factorisation's working planes hold the equilibrated K as well (double-float assembly).
+// *planes_ready: the factorisation's working copy holds the equilibrated K as well (the planes of a
+// double-float assembly, or the FP64 K of an FP64 solve).
 int assemble_stage(const updes_problem* p, const SolveWs& w, int n, int precision, updes_solve_info* info,
                    cudaStream_t s, bool* planes_ready) {
   Timer t(s);
@@ -1062,9 +1071,14 @@ int assemble_stage(const updes_problem* p, const SolveWs& w, int n, int precisio
   UPDES_LAUNCH_CHECK();
   col_scale_kernel<<<unsigned(ceil_div(n, 256)), 256, 0, s>>>(n, w.dc);
   UPDES_LAUNCH_CHECK();
+  // the FP64 path factors the equilibrated FP64 K itself (written back in place), not the 48-bit sum of its
+  // planes: on systems near the FP64 limit (r^5 at N = 10,000) the planes' rounding alone would be 32x the
+  // FP64 rounding of K
+  const int fp64 = precision == UPDES_PREC_FP64;
   split_df_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.W, w.ld, w.Khi, w.Klo, w.ld, n, w.dr,
-                                                                             w.dc);
+                                                                             w.dc, fp64);
   UPDES_LAUNCH_CHECK();
+  *planes_ready = fp64 != 0;  // for the FP64 factorisation: W holds the equilibrated K
   info->t_assemble_ms += t.stop();
   return UPDES_OK;
 }
@@ -1105,7 +1119,14 @@ int solve_stage(const updes_problem* p, const SolveWs& w, int n, const double* q
     if (info->converged || !o.fallback_fp64) break;
     precision = UPDES_PREC_FP64;
     info->fell_back = 1;
-    if ((e = factor_stage(w, n, precision, info, s))) return e;
+    // the FP32 attempt overwrote the working matrix: K is assembled again in FP64 and scaled in place with the
+    // same powers of two, so the fallback factors the FP64 K (not the 48-bit sum of its planes); the planes,
+    // the residuals' operator, stay as they are
+    if ((e = updes_assemble(p, w.W, w.ld, nullptr, 0, s))) return e;
+    split_df_kernel<<<unsigned(ceil_div(int64_t(n) * w.ld, 256)), 256, 0, s>>>(w.W, w.ld, nullptr, nullptr, w.ld, n,
+                                                                               w.dr, w.dc, 1);
+    UPDES_LAUNCH_CHECK();
+    if ((e = factor_stage(w, n, precision, info, s, true))) return e;
   }
   Timer t(s);
   // the values of a mixed-precision solve in double-float (polyharmonic kernels; UPDES_DF_EVAL=0: FP64)

@@ -393,9 +393,15 @@ class DeviceProblem:
         self.kind = torch.as_tensor(np.ascontiguousarray(kind, dtype=np.int32), device=dev)
         self.bnodes = torch.as_tensor(np.ascontiguousarray(bnodes, dtype=np.int32), device=dev)
         self.geom = torch.as_tensor(np.ascontiguousarray(geom, dtype=np.float64), **f64)
+        sup = getattr(cloud, "sorted_local_supports", None)
+        self.supports = None if sup is None else torch.as_tensor(np.ascontiguousarray(sup, dtype=np.int32),
+                                                                 device=dev)
         p = _lib.Problem()
         p.N, p.Ni, p.M, p.rbf, p.rbf_param = self.N, self.Ni, self.M, self.kid, self.param
         p.self_term = int(bool(self_term))
+        if self.supports is not None:
+            p.support_width = int(self.supports.shape[1])
+            p.supports = self.supports.data_ptr()
         p.nodes = self.nodes.data_ptr()
         p.op_weights = self.W.data_ptr() if self.Ni else None
         p.bd_kind = self.kind.data_ptr() if self.N > self.Ni else None
@@ -439,8 +445,10 @@ _FACTOR_CACHE: dict = {}   # (device, slot) -> _Factored
 def _system_key(cloud, rbf, max_degree, W, kind, bnodes, geom, opts):
     import hashlib
     h = hashlib.sha1()
+    sup = getattr(cloud, "sorted_local_supports", None)
     for a in (np.ascontiguousarray(cloud.sorted_nodes), np.ascontiguousarray(W), np.ascontiguousarray(kind),
-              np.ascontiguousarray(bnodes), np.ascontiguousarray(geom)):
+              np.ascontiguousarray(bnodes), np.ascontiguousarray(geom),
+              np.zeros(0, np.int32) if sup is None else np.ascontiguousarray(sup)):
         h.update(a.tobytes())
     return (rbf_spec(rbf), int(max_degree), opts.precision, bool(opts.self_term), h.hexdigest())
 
@@ -593,6 +601,7 @@ def _interp_problem(cloud, rbf, max_degree):
         pass
     c = _C()
     c.N, c.Ni, c.sorted_nodes = cloud.N, 0, cloud.sorted_nodes
+    c.sorted_local_supports = getattr(cloud, "sorted_local_supports", None)  # A's Phi keeps the same supports
     return DeviceProblem(c, rbf, max_degree, np.zeros((0, 5)), kind, nodes, geom)
 
 
@@ -653,6 +662,8 @@ def prepare(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max_de
     N, Ni = cloud.N, cloud.Ni
     X = cloud.sorted_nodes
     M = compute_nb_monomials(max_degree)
+    _require_finite(X, "the cloud's node coordinates")
+    _require_distinct(X)
     fields = None
     if diff_args:
         fields = np.stack([np.asarray(a, dtype=np.float64) for a in diff_args])  # (F, N)
@@ -685,6 +696,19 @@ def prepare(diff_operator, rhs_operator, cloud, boundary_conditions, rbf, max_de
     _require_finite(q, "the right-hand side (rhs_operator and boundary values)")
     _require_finite(geom, "the Robin coefficients")
     return W, kind, bnodes, geom, q
+
+
+def _require_distinct(X):
+    """Two nodes at the same place make two identical rows of the collocation matrix: it is singular, and an
+    LU then meets a pivot at rounding level rather than an exact zero (LAPACK's too), so the solve would
+    return noise.  Rejected on the host (the reference solves it silently)."""
+    order = np.lexsort((X[:, 1], X[:, 0]))
+    same = np.all(X[order[1:]] == X[order[:-1]], axis=1)
+    if np.any(same):
+        k = int(np.flatnonzero(same)[0])
+        i, j = sorted((int(order[k]), int(order[k + 1])))
+        raise ValueError(f"nodes {i} and {j} (sorted order) coincide at {tuple(X[i])}: the collocation matrix "
+                         f"would be singular")
 
 
 def _require_finite(a, what):
