@@ -327,6 +327,34 @@ UPDES_API int updes_solve_many(const updes_problem* problems, int32_t count, con
                                double* const* coeffs, double* const* vals, const updes_solve_opts* opts,
                                updes_solve_info* infos, void* workspace, size_t workspace_bytes, int32_t streams);
 
+/*
+ * Many independent systems in ONE persistent launch.  `ctas` CTAs (0 = one
+ * per SM) take systems from a device work queue, largest first, and each CTA
+ * runs a system's whole solve by itself: assembly of K (FP64, equilibrated by
+ * powers of two) and of the value rows [Phi P]; LU with partial pivoting in
+ * panels of panel_width[i] columns (1..64, NULL = 16; chosen per system size
+ * by the caller's autotuner) in double-float arithmetic on the FP32 pipes
+ * (precision[i] = UPDES_PREC_FP32, about 48-bit factors) or in FP64
+ * (UPDES_PREC_FP64) (precision NULL = all FP32); then classical refinement
+ * sweeps with an FP64 residual, at most max_sweeps, until the componentwise
+ * backward error reaches 32 FP64 unit roundoffs or stops halving; coeffs[i]
+ * (n_i) and vals[i] (N_i; vals or vals[i] may be NULL).  infos (may be NULL):
+ * iters = refinement sweeps, lu_info, converged, backward_error.  Systems
+ * must have N + M <= 4096 and no local supports (UPDES_ERR_UNSUPPORTED
+ * otherwise).  No CTA waits for another.  The call synchronises `stream`; a
+ * singular system gives UPDES_ERR_SINGULAR (the others are still solved).
+ * workspace: updes_solve_batched_workspace bytes (per CTA, K, the working
+ * matrix and the value rows of the largest system: about 24 n_max^2 bytes).
+ * The reference runs one pde_solver call per system
+ * (updes/operators.py:559-618).
+ */
+UPDES_API int updes_solve_batched_workspace(const updes_problem* problems, int32_t count, int32_t ctas,
+                                            size_t* bytes);
+UPDES_API int updes_solve_batched(const updes_problem* problems, int32_t count, const double* const* q,
+                                  double* const* coeffs, double* const* vals, const int32_t* precision,
+                                  const int32_t* panel_width, int32_t max_sweeps, int32_t ctas,
+                                  updes_solve_info* infos, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---- adjoint (reverse mode through the solve) ------------------------------
  * The reference differentiates pde_solver with jax.grad through inv, the GEMM
  * and the lineax QR (demos/Laplace/10_laplace_with_diff_phys.py:89-104) or runs

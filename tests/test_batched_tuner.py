@@ -1,0 +1,35 @@
+"""CPU: the batched solver's panel-width autotuner (keys, choice, JSON cache) and its size buckets."""
+import json
+
+import pytest
+
+from updes_gb300.batched import PanelTuner, size_bucket
+
+
+def test_tuner_picks_the_fastest_and_caches(tmp_path):
+    path = str(tmp_path / "widths.json")
+    calls = []
+
+    def measure(w):
+        calls.append(w)
+        return {16: 3.0, 32: 1.5, 64: 2.0}[w]
+
+    t = PanelTuner(cache_path=path)
+    key = PanelTuner.key("GB300", 0, "fp32", 1024)
+    assert t.width(key, measure) == 32
+    assert calls == [16, 32, 64]
+    assert t.width(key, measure) == 32 and calls == [16, 32, 64]  # cached: no new measurement
+    assert json.load(open(path)) == {key: 32}
+    t2 = PanelTuner(cache_path=path)  # a new process reads the file
+    assert t2.width(key, lambda w: pytest.fail("should not measure")) == 32
+
+
+def test_tuner_ties_prefer_the_narrower_panel_and_memory_only_cache():
+    t = PanelTuner(cache_path=None)
+    assert t.width(PanelTuner.key("g", 1, "fp64", 256), lambda w: 1.0) == 16
+
+
+def test_size_buckets():
+    assert size_bucket(106) == 256 and size_bucket(257) == 512 and size_bucket(2031) == 2048
+    with pytest.raises(ValueError):
+        size_bucket(4097)

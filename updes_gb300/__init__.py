@@ -13,6 +13,7 @@ from .operators import (
     nodal_div_grad, nodal_gradient, nodal_laplacian, nodal_value, pde_multi_solver, pde_solver, pde_solver_jit,
     pde_solver_many, pde_solver_jit_with_bc, value, value_vec,
 )
+from .batched import PanelTuner, pde_solver_batched
 from .rbf import distance, gaussian, inverse_multiquadric, multiquadric, polyharmonic, rbf_spec, thin_plate
 
 __version__ = "0.1.0"

@@ -115,6 +115,9 @@ SIGNATURES = {
                                                   ctypes.POINTER(_sz)]),
     "updes_solve_many": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _vp, _vp, ctypes.POINTER(SolveOpts),
                                         ctypes.POINTER(SolveInfo), _vp, _sz, _i32]),
+    "updes_solve_batched_workspace": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _i32, ctypes.POINTER(_sz)]),
+    "updes_solve_batched": (ctypes.c_int, [ctypes.POINTER(Problem), _i32, _vp, _vp, _vp, _vp, _vp, _i32, _i32,
+                                           ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),
     "updes_eval_values_t": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, _vp]),
     "updes_solve_transpose": (ctypes.c_int, [ctypes.POINTER(Problem), _vp, _vp, ctypes.POINTER(SolveOpts),
                                              ctypes.POINTER(SolveInfo), _vp, _sz, _vp]),

@@ -1,0 +1,268 @@
+"""Many independent systems in one persistent launch, with a panel-width autotuner.
+
+The reference solves each system with its own ``pde_solver`` call (updes/operators.py:559-618).
+``pde_solver_batched`` prepares every system on the host exactly as ``pde_solver`` does (operator capture,
+boundary rows, right-hand side) and hands them all to ``updes_solve_batched``: one CTA per SM takes systems
+from a device work queue, largest first, and runs each one's assembly, LU, refinement and values by itself.
+
+Precision per system:
+
+* ``"fp32"`` -- the elimination in double-float arithmetic on the FP32 pipes (about 48-bit factors) with
+  classical refinement sweeps on an FP64 residual;
+* ``"fp64"`` -- the elimination in FP64;
+* ``"auto"`` (default) -- ``"fp32"`` first.  Refinement stops at a componentwise backward error of 32 FP64
+  unit roundoffs, or where it stops halving: beyond a condition number of about 2^48 the 48-bit factors
+  no longer contract the error, and the answer keeps the backward error the elimination gave it (a few
+  1e-14 on the uneven-cloud workload's flattest Gaussian systems, whose forward error no FP64 solver
+  bounds either).  A system whose backward error stays above ``RELAUNCH_BACKWARD_ERROR`` (1e-12), or whose
+  elimination met a zero pivot, is solved again in FP64 in a second launch of only those systems.
+
+The autotuner (``PanelTuner``) picks the LU panel width per (GPU, kernel, precision, size bucket): it times
+one launch on a single CTA for each candidate width on the largest system of the bucket in the batch, keeps
+the fastest, and caches the choice in memory and, unless disabled, in a JSON file
+(``$UPDES_TUNE_CACHE`` or ``~/.cache/updes_gb300/panel_widths.json``).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+import threading
+
+from . import _lib
+from .operators import (DEFAULT_OPTIONS, CollocationMatrix, DeviceProblem, SteadySol, _torch,
+                        boundary_conditions_func_to_arr, materialize_B, prepare)
+
+PANEL_CANDIDATES = (16, 32, 64)
+SIZE_BUCKETS = (256, 512, 1024, 2048, 4096)
+MAX_N = 4096
+RELAUNCH_BACKWARD_ERROR = 1e-12
+LAST_BATCHED_INFO: list = []
+LAST_BATCHED_TIMING: dict = {}
+
+
+def size_bucket(n: int) -> int:
+    for b in SIZE_BUCKETS:
+        if n <= b:
+            return b
+    raise ValueError(f"systems of n = {n} unknowns exceed the batched solver's limit of {MAX_N}")
+
+
+def _default_cache_path():
+    path = os.environ.get("UPDES_TUNE_CACHE")
+    if path is not None:
+        return path or None  # an empty value disables the file cache
+    return os.path.join(os.path.expanduser("~"), ".cache", "updes_gb300", "panel_widths.json")
+
+
+class PanelTuner:
+    """Panel widths of the batched LU by (GPU, kernel, precision, size bucket), measured on first use.
+
+    ``measure(width) -> milliseconds`` is supplied by the caller for the system that represents a bucket; the tuner calls it for every candidate and keeps the fastest.  Choices persist in
+    ``cache_path`` (JSON; None keeps them in memory only).
+    """
+
+    def __init__(self, cache_path="default", candidates=PANEL_CANDIDATES):
+        self.cache_path = _default_cache_path() if cache_path == "default" else cache_path
+        self.candidates = tuple(candidates)
+        self._lock = threading.Lock()
+        self.table = {}
+        self.measurements = {}
+        if self.cache_path and os.path.exists(self.cache_path):
+            try:
+                with open(self.cache_path) as fh:
+                    self.table = {k: int(v) for k, v in json.load(fh).items()}
+            except (OSError, ValueError):
+                self.table = {}
+
+    @staticmethod
+    def key(gpu: str, kind: int, precision: str, bucket: int) -> str:
+        return f"{gpu}|rbf{kind}|{precision}|n<={bucket}"
+
+    def width(self, key: str, measure) -> int:
+        with self._lock:
+            if key in self.table:
+                return self.table[key]
+        times = {w: float(measure(w)) for w in self.candidates}
+        best = min(times, key=lambda w: (times[w], w))
+        with self._lock:
+            self.table[key] = best
+            self.measurements[key] = times
+            self._save()
+        return best
+
+    def _save(self):
+        if not self.cache_path:
+            return
+        try:
+            os.makedirs(os.path.dirname(self.cache_path), exist_ok=True)
+            tmp = self.cache_path + ".tmp"
+            with open(tmp, "w") as fh:
+                json.dump(self.table, fh, indent=1, sort_keys=True)
+            os.replace(tmp, self.cache_path)
+        except OSError:
+            pass  # a read-only home directory keeps the choices in memory
+
+
+_TUNER = None
+
+
+def default_tuner() -> PanelTuner:
+    global _TUNER
+    if _TUNER is None:
+        _TUNER = PanelTuner()
+    return _TUNER
+
+
+class _Batch:
+    """Device arrays and C structs of one batch (kept alive while the library uses them)."""
+
+    def __init__(self, dps, qs):
+        torch = _torch()
+        self.torch = torch
+        self.dps, self.qs = dps, qs
+        self.count = len(dps)
+        dev = dps[0].device
+        self.coeffs = [torch.empty(dp.n, dtype=torch.float64, device=dev) for dp in dps]
+        self.vals = [torch.empty(dp.N, dtype=torch.float64, device=dev) for dp in dps]
+        c = self.count
+        self.probs = (_lib.Problem * c)(*[dp.c for dp in dps])
+        ptrs = lambda ts: (ctypes.c_void_p * c)(*[t.data_ptr() for t in ts])
+        self.qp, self.cp, self.vp = ptrs(qs), ptrs(self.coeffs), ptrs(self.vals)
+        self.infos = (_lib.SolveInfo * c)()
+
+    def run(self, idx, precisions, widths, max_sweeps, ctas):
+        """Solve the systems ``idx`` (host indices into the batch) in one launch; returns the status."""
+        torch, lib = self.torch, _lib.load()
+        c = len(idx)
+        sub = lambda arr, T: (T * c)(*[arr[i] for i in idx])
+        probs = sub(self.probs, _lib.Problem)
+        qp, cp, vp = sub(self.qp, ctypes.c_void_p), sub(self.cp, ctypes.c_void_p), sub(self.vp, ctypes.c_void_p)
+        prec = (ctypes.c_int32 * c)(*[precisions[i] for i in idx])
+        wid = (ctypes.c_int32 * c)(*[widths[i] for i in idx])
+        infos = (_lib.SolveInfo * c)()
+        nbytes = ctypes.c_size_t()
+        _lib.check(lib.updes_solve_batched_workspace(probs, c, int(ctas), ctypes.byref(nbytes)),
+                   "updes_solve_batched_workspace")
+        ws = _workspace(nbytes.value, self.dps[0].device)
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        st = lib.updes_solve_batched(probs, c, ctypes.cast(qp, ctypes.c_void_p), ctypes.cast(cp, ctypes.c_void_p),
+                                     ctypes.cast(vp, ctypes.c_void_p), prec, wid, int(max_sweeps), int(ctas), infos,
+                                     ws.data_ptr(), ws.numel(), stream)
+        for k, i in enumerate(idx):
+            self.infos[i] = infos[k]
+        return st
+
+
+_WS: dict = {}
+
+
+def _workspace(nbytes, device):
+    torch = _torch()
+    buf = _WS.get(device.index)
+    if buf is None or buf.numel() < nbytes:
+        _WS.pop(device.index, None)
+        buf = torch.empty(int(nbytes), dtype=torch.uint8, device=device)
+        _WS[device.index] = buf
+    return buf
+
+
+def free_workspace():
+    _WS.clear()
+
+
+def _tune_widths(batch, precisions, tuner, max_sweeps):
+    """Panel width per system from the tuner, measuring each new (kernel, precision, bucket) on the largest
+    system of that bucket in the batch with one CTA."""
+    torch = batch.torch
+    gpu = torch.cuda.get_device_name(batch.dps[0].device)
+    groups = {}
+    for i, dp in enumerate(batch.dps):
+        key = PanelTuner.key(gpu, dp.kid, "fp64" if precisions[i] == _lib.PREC_FP64 else "fp32", size_bucket(dp.n))
+        if key not in groups or dp.n > batch.dps[groups[key]].n:
+            groups[key] = i
+    widths = [16] * batch.count
+    chosen = {}
+    for key, rep in groups.items():
+        def measure(w, rep=rep):
+            ws = [w] * batch.count
+            batch.run([rep], precisions, ws, max_sweeps, 1)  # loads the kernel, touches the workspace
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            batch.run([rep], precisions, ws, max_sweeps, 1)
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+        chosen[key] = tuner.width(key, measure)
+    for i, dp in enumerate(batch.dps):
+        key = PanelTuner.key(gpu, dp.kid, "fp64" if precisions[i] == _lib.PREC_FP64 else "fp32", size_bucket(dp.n))
+        widths[i] = chosen[key]
+    return widths
+
+
+def pde_solver_batched(systems, options=None, precision="auto", max_sweeps=4, ctas=0, tuner="default"):
+    """Solve many independent systems in one persistent launch (``updes_solve_batched``).
+
+    ``systems``: dicts with the keyword arguments of ``pde_solver`` (as for ``pde_solver_many``); callable
+    boundary conditions are evaluated as in ``pde_solver_jit``.  ``precision``: ``"auto"``, ``"fp32"``,
+    ``"fp64"`` or one of them per system.  ``tuner``: a ``PanelTuner``, ``"default"`` (the process-wide one)
+    or None (panel width 16 everywhere).  Returns a list of ``SteadySol`` in the order of ``systems``;
+    ``LAST_BATCHED_INFO`` holds each solve's report (sweeps, converged, backward_error, precision used).
+    """
+    import time
+    torch = _torch()
+    opts = options or DEFAULT_OPTIONS
+    t0 = time.perf_counter()
+    dps, qs = [], []
+    for sysd in systems:
+        cloud = sysd["cloud"]
+        bcs = boundary_conditions_func_to_arr(sysd["boundary_conditions"], cloud)
+        W, kind, bnodes, geom, q = prepare(sysd["diff_operator"], sysd["rhs_operator"], cloud, bcs, sysd["rbf"],
+                                           sysd["max_degree"], sysd.get("diff_args"), sysd.get("rhs_args"), opts)
+        dp = DeviceProblem(cloud, sysd["rbf"], sysd["max_degree"], W, kind, bnodes, geom, opts.self_term)
+        if dp.n > MAX_N:
+            raise ValueError(f"system of n = {dp.n} unknowns exceeds the batched solver's limit of {MAX_N}")
+        dps.append(dp)
+        qs.append(torch.as_tensor(q, dtype=torch.float64, device=dp.device))
+    if not dps:
+        return []
+    batch = _Batch(dps, qs)
+    names = precision if isinstance(precision, (list, tuple)) else [precision] * len(dps)
+    code = {"fp32": _lib.PREC_FP32, "auto": _lib.PREC_FP32, "fp64": _lib.PREC_FP64}
+    precs = [code[p] for p in names]
+    tuner = default_tuner() if tuner == "default" else tuner
+    widths = _tune_widths(batch, precs, tuner, max_sweeps) if tuner is not None else [16] * len(dps)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record()
+    st = batch.run(list(range(len(dps))), precs, widths, max_sweeps, ctas)
+    e1.record()
+    used = ["fp64" if p == _lib.PREC_FP64 else "fp32" for p in precs]
+    redo = [i for i, nm in enumerate(names) if nm == "auto" and (batch.infos[i].lu_info != 0 or not
+                                                                  batch.infos[i].backward_error <= RELAUNCH_BACKWARD_ERROR)]
+    if redo:
+        precs2 = list(precs)
+        for i in redo:
+            precs2[i] = _lib.PREC_FP64
+            used[i] = "fp64 (after fp32)"
+        w2 = _tune_widths(batch, precs2, tuner, max_sweeps) if tuner is not None else widths
+        e1.record()
+        st2 = batch.run(redo, precs2, w2, max_sweeps, ctas)
+        if st == _lib.OK or st == _lib.ERR_SINGULAR:
+            st = st2 if st2 != _lib.OK else st
+    e2.record()
+    torch.cuda.synchronize()
+    LAST_BATCHED_TIMING.clear()
+    LAST_BATCHED_TIMING.update(host_prepare_s=t1 - t0, launch_ms=e0.elapsed_time(e1),
+                               fp64_relaunch_ms=e1.elapsed_time(e2), relaunched=len(redo))
+    LAST_BATCHED_INFO[:] = [dict(batch.infos[i].as_dict(), precision=used[i], panel_width=widths[i])
+                            for i in range(len(dps))]
+    _lib.check(st, "updes_solve_batched")
+    out = []
+    for sysd, dp, c, v in zip(systems, dps, batch.coeffs, batch.vals):
+        cloud, rbf, deg = sysd["cloud"], sysd["rbf"], sysd["max_degree"]
+        out.append(SteadySol(v.cpu().numpy(), c.cpu().numpy(),
+                             CollocationMatrix(lambda dp=dp, cloud=cloud, rbf=rbf, deg=deg:
+                                               materialize_B(dp, cloud, rbf, deg))))
+    return out

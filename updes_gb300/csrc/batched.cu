@@ -12,9 +12,9 @@
 //              pipes (UPDES_PREC_FP32: about 48-bit factors, GB300's FP64 pipe is 1/64 of its FP32 rate) or
 //              in FP64 (UPDES_PREC_FP64)
 //   refinement y = (LU)^-1 b, then classical refinement sweeps y += (LU)^-1 (b - K y) with an FP64 residual
-//              until the componentwise backward error reaches 256 FP64 unit roundoffs, stops falling, or the
-//              sweep cap is met; with 48-bit factors one or two sweeps reach the FP64 floor wherever
-//              cond(K) * 2^-48 < 1
+//              until the componentwise backward error reaches 32 FP64 unit roundoffs, stops halving, or the
+//              sweep cap is met; with 48-bit factors each sweep gains a factor of about 1 / (cond(K) 2^-48),
+//              so one or two sweeps reach the floor wherever cond(K) 2^-48 is small
 //   values     coeffs = Dc y, vals = A[:N] coeffs
 //
 // The CTA's scratch (its slice of the workspace) holds K, the working matrix and A for the largest system.
@@ -38,9 +38,11 @@ namespace {
 constexpr int kBT = 512;                 // threads per CTA
 constexpr int kWarps = kBT / 32;
 constexpr int kTM = 128, kTN = 64;       // trailing-update tile: 4 x 4 entries per thread
-constexpr int kMaxNB = 32;               // widest panel
+constexpr int kMaxNB = 64;               // widest panel
 constexpr int kMaxBatchN = 4096;         // the solve's vectors live in shared memory
-constexpr double kBwdFloorB = 256.0 * 1.1102230246251565e-16;
+// Refinement stops at a componentwise backward error of 32 FP64 unit roundoffs: the residual is FP64 here
+// (K is kept in FP64), so the floor sits just above the residual's own rounding over a few thousand terms.
+constexpr double kBwdFloorB = 32.0 * 1.1102230246251565e-16;
 
 struct BatchSys {
   updes_problem p;
