@@ -336,8 +336,9 @@ UPDES_API int updes_solve_many(const updes_problem* problems, int32_t count, con
  * by the caller's autotuner) in double-float arithmetic on the FP32 pipes
  * (precision[i] = UPDES_PREC_FP32, about 48-bit factors) or in FP64
  * (UPDES_PREC_FP64) (precision NULL = all FP32); then classical refinement
- * sweeps with an FP64 residual, at most max_sweeps, until the componentwise
- * backward error reaches 32 FP64 unit roundoffs or stops halving; coeffs[i]
+ * sweeps with an FP64 residual, at most max_sweeps, while the componentwise
+ * backward error still halves (down to 2 FP64 unit roundoffs; converged = at
+ * most 32); coeffs[i]
  * (n_i) and vals[i] (N_i; vals or vals[i] may be NULL).  infos (may be NULL):
  * iters = refinement sweeps, lu_info, converged, backward_error.  Systems
  * must have N + M <= 4096 and no local supports (UPDES_ERR_UNSUPPORTED

@@ -10,8 +10,8 @@ Precision per system:
 * ``"fp32"`` -- the elimination in double-float arithmetic on the FP32 pipes (about 48-bit factors) with
   classical refinement sweeps on an FP64 residual;
 * ``"fp64"`` -- the elimination in FP64;
-* ``"auto"`` (default) -- ``"fp32"`` first.  Refinement stops at a componentwise backward error of 32 FP64
-  unit roundoffs, or where it stops halving: beyond a condition number of about 2^48 the 48-bit factors
+* ``"auto"`` (default) -- ``"fp32"`` first.  Refinement goes on while the componentwise backward error
+  still halves (converged: at most 32 FP64 unit roundoffs): beyond a condition number of about 2^48 the 48-bit factors
   no longer contract the error, and the answer keeps the backward error the elimination gave it (a few
   1e-14 on the uneven-cloud workload's flattest Gaussian systems, whose forward error no FP64 solver
   bounds either).  A system whose backward error stays above ``RELAUNCH_BACKWARD_ERROR`` (1e-12), or whose
