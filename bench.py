@@ -390,6 +390,21 @@ def profile_solve(args):
                                                                             "backward_error")}}}), flush=True)
 
 
+def profile_batched(args):
+    """One persistent launch (mixed precision, panel width 32, no autotuning) over the first
+    ``--profile-batched`` systems of the uneven-cloud workload, and nothing else: the launch a profiler
+    capture of batched_solve_kernel expects."""
+    import torch
+
+    import updes_gb300 as U
+    from updes_gb300 import batched as B
+    from updes_gb300 import workloads as WL
+    systems = WL.uneven_clouds(args.batch_count)[:args.profile_batched]
+    U.pde_solver_batched(systems, precision="fp32", tuner=B.PanelTuner(cache_path=None, candidates=(32,)))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_batched": {"systems": len(systems), **B.LAST_BATCHED_TIMING}}), flush=True)
+
+
 def extra_configs(args, U, torch):
     """The other benchmark configurations, each bounded to seconds, measured with CUDA events (device work)
     on the current stream or the wall clock around a synchronised call (noted per entry).  A configuration
@@ -560,9 +575,14 @@ def main():
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--profile-solve", action="store_true",
                     help="run one mixed solve and exit (the launch order a profiler capture expects)")
+    ap.add_argument("--profile-batched", type=int, default=0,
+                    help="run one persistent launch over this many uneven clouds and exit")
     args = ap.parse_args()
     if args.profile_solve:
         profile_solve(args)
+        return
+    if args.profile_batched:
+        profile_batched(args)
         return
     if args.warmup < 3:
         args.warmup = 3

@@ -153,11 +153,25 @@ __device__ void assemble_system(const BatchSys& sys, double* K, double* A, int64
   for (int r = warp; r < n; r += kWarps) {
     const RowInfo ri = load_row(p, r);
     double* Kr = K + int64_t(r) * ld;
+    double* Ar = A + int64_t(r) * ld;
+    // the value row of node r, A[r] = [phi(x_r - x_j) (0 at j = r), m_k(x_r)], from the same kernel
+    // evaluations as K's row where the row's evaluation node is r
+    const bool fused = r < p.N && ri.a == r;
     double mx = 0.0;
     for (int c = lane; c < n; c += 32) {
       double v;
-      if (c < p.N) v = entry_rbf<KIND>(ri, c, p.nodes[2ll * c], p.nodes[2ll * c + 1], p.rbf_param, ip, p.self_term);
-      else v = entry_mono(ri, c - p.N);
+      if (c < p.N) {
+        const double xc = p.nodes[2ll * c], yc = p.nodes[2ll * c + 1];
+        if (fused) {
+          double phi;
+          v = entry_rbf_phi<KIND>(ri, c, xc, yc, p.rbf_param, ip, p.self_term, &phi);
+          Ar[c] = phi;
+        } else {
+          v = entry_rbf<KIND>(ri, c, xc, yc, p.rbf_param, ip, p.self_term);
+        }
+      } else {
+        v = entry_mono(ri, c - p.N);
+      }
       Kr[c] = v;
       mx = fmax(mx, fabs(v));
     }
@@ -168,14 +182,12 @@ __device__ void assemble_system(const BatchSys& sys, double* K, double* A, int64
       dr[r] = s;
       b[r] = r < p.N ? s * sys.q[r] : 0.0;
     }
-    if (r < p.N) {  // the value row of node r: A[r] = [phi(x_r - x_j) (0 at j = r), m_k(x_r)]
-      double* Ar = A + int64_t(r) * ld;
+    if (r < p.N) {
       const double xr = p.nodes[2ll * r], yr = p.nodes[2ll * r + 1];
       for (int c = lane; c < n; c += 32) {
-        double v;
-        if (c < p.N) v = (c == r && !p.self_term) ? 0.0 : rbf_value<KIND>(xr - p.nodes[2ll * c], yr - p.nodes[2ll * c + 1], p.rbf_param, ip);
-        else v = monomial_terms(c - p.N, xr, yr).m;
-        Ar[c] = v;
+        if (c >= p.N) Ar[c] = monomial_terms(c - p.N, xr, yr).m;
+        else if (!fused)
+          Ar[c] = (c == r && !p.self_term) ? 0.0 : rbf_value<KIND>(xr - p.nodes[2ll * c], yr - p.nodes[2ll * c + 1], p.rbf_param, ip);
       }
     }
   }
@@ -221,15 +233,17 @@ __device__ int cta_lu(typename Ops::T* W, int64_t ld, int n, int nb, int32_t* pi
   for (int k0 = 0; k0 < n; k0 += nb) {
     const int kb = min(nb, n - k0);
     const int k1 = k0 + kb;
-    // ---- panel: columns [k0, k1), rows [k0, n)
+    // ---- panel: columns [k0, k1), rows [k0, n).  One thread per row for the scaling and the rank-1
+    // update (its row's panel entries are adjacent, so after the first access they come from L1, and the
+    // CTA's 512 rows are in flight at once); the candidate for the next column's pivot is taken on the way.
+    double bv = -1.0;
+    int bi = n;
+    for (int i = k0 + tid; i < n; i += kBT) {
+      double v = fabs(Ops::to_d(W[int64_t(i) * ld + k0]));
+      if (v != v) v = INFINITY;  // NaN wins, so it surfaces as a bad pivot
+      if (v > bv) { bv = v; bi = i; }
+    }
     for (int j = k0; j < k1; ++j) {
-      double bv = -1.0;
-      int bi = n;
-      for (int i = j + tid; i < n; i += kBT) {
-        double v = fabs(Ops::to_d(W[int64_t(i) * ld + j]));
-        if (v != v) v = INFINITY;  // NaN wins, so it surfaces as a bad pivot
-        if (v > bv) { bv = v; bi = i; }
-      }
       cta_argmax(bv, bi, red_v, red_i);
       const int p = bi < n ? bi : j;
       if (p != j)
@@ -249,15 +263,32 @@ __device__ int cta_lu(typename Ops::T* W, int64_t ld, int n, int nb, int32_t* pi
       }
       for (int c = j + 1 + tid; c < k1; c += kBT) prow[c - k0] = W[int64_t(j) * ld + c];
       __syncthreads();
-      if (ok) {
-        const T inv = Ops::from_d(1.0 / pv);
-        // rows below: scale column j, rank-1 update of the panel's columns (j, k1); one warp per row
-        for (int i = j + 1 + warp; i < n; i += kWarps) {
-          T* Wi = W + int64_t(i) * ld;
-          const T l = Ops::mul(Wi[j], inv);
-          for (int c = j + 1 + lane; c < k1; c += 32) Ops::fms(Wi[c], l, prow[c - k0]);
-          __syncwarp();
-          if (lane == 0) Wi[j] = l;
+      bv = -1.0;
+      bi = n;
+      const T inv = Ops::from_d(ok ? 1.0 / pv : 0.0);
+      // rows below: scale column j and update the panel's columns (j, k1), one thread per row; the row's
+      // remaining panel entries are loaded together (one round trip), updated in a local copy and stored
+      // back, and the candidate for the next column's pivot is taken on the way.  (A warp-per-row mapping
+      // with coalesced accesses and eight rows in flight per warp measured slower on GB300.)
+      for (int i = j + 1 + tid; i < n; i += kBT) {
+        T* Wi = W + int64_t(i) * ld;
+        if (ok) {
+          T rowv[kMaxNB];
+          const int cnt = k1 - j;  // columns j .. k1 - 1
+          for (int c = 0; c < cnt; ++c) rowv[c] = Wi[j + c];
+          const T l = Ops::mul(rowv[0], inv);
+          rowv[0] = l;
+          for (int c = 1; c < cnt; ++c) Ops::fms(rowv[c], l, prow[j + c - k0]);
+          for (int c = 0; c < cnt; ++c) Wi[j + c] = rowv[c];
+          if (cnt > 1) {
+            double v = fabs(Ops::to_d(rowv[1]));
+            if (v != v) v = INFINITY;
+            if (v > bv) { bv = v; bi = i; }
+          }
+        } else if (j + 1 < k1) {
+          double v = fabs(Ops::to_d(Wi[j + 1]));
+          if (v != v) v = INFINITY;
+          if (v > bv) { bv = v; bi = i; }
         }
       }
       __syncthreads();

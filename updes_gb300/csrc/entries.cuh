@@ -84,6 +84,35 @@ __device__ __forceinline__ double entry_rbf(const RowInfo& ri, int c, double xc,
   return ga.g1 * (ri.n1x * dx + ri.n1y * dy) + gb.g1 * (ri.n2x * ex + ri.n2y * ey);
 }
 
+// entry_rbf for a row whose evaluation node is also its value row's node (every row r < N but the periodic
+// flux rows), returning as well the value-row entry A[a][c] = phi(x_a - x_c) (0 at c = a unless self_term)
+// from the same kernel evaluation.
+template <int KIND>
+__device__ __forceinline__ double entry_rbf_phi(const RowInfo& ri, int c, double xc, double yc, double param,
+                                                int ip, int self_term, double* phi) {
+  const double dx = ri.xa - xc, dy = ri.ya - yc;
+  const double r2 = dx * dx + dy * dy;
+  if (c == ri.a && !self_term) {
+    *phi = 0.0;
+    if (ri.kind == UPDES_ROW_PERIODIC_VALUE || ri.kind == UPDES_ROW_PERIODIC_FLUX)
+      return entry_rbf<KIND>(ri, c, xc, yc, param, ip, self_term);
+    return 0.0;
+  }
+  if (ri.kind == UPDES_ROW_PERIODIC_VALUE || ri.kind == UPDES_ROW_PERIODIC_FLUX || r2 == 0.0) {
+    *phi = r2 == 0.0 ? rbf_phi0<KIND>() : rbf_g<KIND>(r2, param, ip).phi;
+    return entry_rbf<KIND>(ri, c, xc, yc, param, ip, self_term);
+  }
+  const RbfG g = rbf_g<KIND>(r2, param, ip);
+  *phi = g.phi;
+  if (ri.kind == -1)
+    return ri.w0 * g.phi + g.g1 * (ri.w1 * dx + ri.w2 * dy + (ri.w3 + ri.w4)) +
+           g.g2 * (ri.w3 * dx * dx + ri.w4 * dy * dy);
+  if (ri.kind == UPDES_ROW_DIRICHLET) return g.phi;
+  const double fl = g.g1 * (ri.n1x * dx + ri.n1y * dy);
+  if (ri.kind == UPDES_ROW_NEUMANN) return fl;
+  return ri.beta * g.phi + fl;
+}
+
 // Entry (row, monomial column k) of K.
 __device__ __forceinline__ double entry_mono(const RowInfo& ri, int k) {
   if (ri.kind == -2) return 0.0;
