@@ -1643,10 +1643,21 @@ constexpr int kTB2 = 2 * kTB;
 constexpr int kT2S = kTB2 + 2;  // even row stride: column pairs load as aligned 8-byte vectors
 constexpr size_t kTrsv128Smem = sizeof(float) * 3 * size_t(kTB2) * kT2S;
 
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// With xtag, a solved block hands its x to the blocks after it through tagged words: row i's hi and lo parts
+// go to xtag[2i] and xtag[2i + 1] as (block + 1) << 32 | float bits, each one single-copy-atomic 8-byte store,
+// so a reader that sees its block's tag has the value, with no flag, no fence and no second round trip.  The
+// words are cleared before every call, so a tag can only come from the current call.
 template <int MODE>
 __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restrict__ F, int64_t ldf, int n, double* x,
                                                           float* xh_g, float* xl_g, int* ticket, int* flags,
-                                                          DeviceStatus* st, const float* __restrict__ dinv128) {
+                                                          DeviceStatus* st, const float* __restrict__ dinv128,
+                                                          unsigned long long* xtag) {
   extern __shared__ __align__(16) unsigned char t128_smem[];
   float(*sT)[kT2S] = reinterpret_cast<float(*)[kT2S]>(t128_smem);
   float(*sDh)[kT2S] = sT + kTB2;
@@ -1722,29 +1733,56 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
   for (int q = 0; q < t; ++q) {
     const int c0 = tile_cols(q);
     const int cols = min(kTB2, n - c0);
-    if (tid == 0 && s_done <= q) {
-      // acquire loads of the count of finished blocks: they synchronise with each block's fence and increment,
-      // and the CTA barrier below carries that order to the threads that then read x
-      const int* vc = flags + nblk;
-      long long it = 0;
-      int d;
-      while ((d = ld_acquire_gpu(vc)) <= q) {
-        if (++it > spin_limit()) {
-          status_error(st, UPDES_ERR_TIMEOUT);
-          atomicCAS(&st->timeout_tag, 0, 30 + MODE);
-          d = q + 1;
-          break;
+    if (xtag) {
+      // tile q is in sT (stored in the previous round, before the barrier that ended it); each of 256
+      // threads waits (bounded) for one word of block q's x
+      if (tid < 2 * kTB2) {
+        const int rr = tid >> 1;
+        float v = 0.f;
+        if (rr < cols) {
+          const unsigned want = unsigned(c0 / kTB2 + 1);
+          const unsigned long long* p = xtag + 2ll * (c0 + rr) + (tid & 1);
+          unsigned long long w = ld_relaxed_u64(p);
+          long long it = 0;
+          while (unsigned(w >> 32) != want) {
+            if (++it > spin_limit()) {
+              status_error(st, UPDES_ERR_TIMEOUT);
+              atomicCAS(&st->timeout_tag, 0, 40 + MODE);
+              break;
+            }
+            if (it > 32) __nanosleep(20);
+            w = ld_relaxed_u64(p);
+          }
+          v = __uint_as_float(unsigned(w));
         }
-        __nanosleep(20);
+        ((tid & 1) ? sxl : sxh)[rr] = v;
       }
-      s_done = d;
+      __syncthreads();
+    } else {
+      if (tid == 0 && s_done <= q) {
+        // acquire loads of the count of finished blocks: they synchronise with each block's fence and increment,
+        // and the CTA barrier below carries that order to the threads that then read x
+        const int* vc = flags + nblk;
+        long long it = 0;
+        int d;
+        while ((d = ld_acquire_gpu(vc)) <= q) {
+          if (++it > spin_limit()) {
+            status_error(st, UPDES_ERR_TIMEOUT);
+            atomicCAS(&st->timeout_tag, 0, 30 + MODE);
+            d = q + 1;
+            break;
+          }
+          __nanosleep(20);
+        }
+        s_done = d;
+      }
+      __syncthreads();  // tile q is in sT (stored in the previous round); block q is solved
+      if (tid < kTB2) {
+        sxh[tid] = tid < cols ? __ldcg(xh_g + c0 + tid) : 0.f;
+        sxl[tid] = tid < cols ? __ldcg(xl_g + c0 + tid) : 0.f;
+      }
+      __syncthreads();
     }
-    __syncthreads();  // tile q is in sT (stored in the previous round); block q is solved
-    if (tid < kTB2) {
-      sxh[tid] = tid < cols ? __ldcg(xh_g + c0 + tid) : 0.f;
-      sxl[tid] = tid < cols ? __ldcg(xl_g + c0 + tid) : 0.f;
-    }
-    __syncthreads();
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       const int c = part * 32 + 2 * ((k + 4 * part) & 15);  // column pair, rotated per part
@@ -1785,10 +1823,17 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
   df_add_to(ph, pl, dh2.y, dl2.y);
   df_quad_sum(ph, pl);
   if (part == 0 && row < rows) {
-    xh_g[r0 + row] = ph;
-    xl_g[r0 + row] = pl;
+    if (xtag) {
+      const unsigned long long tag = (unsigned long long)(unsigned)(blk + 1) << 32;
+      xtag[2ll * (r0 + row)] = tag | __float_as_uint(ph);
+      xtag[2ll * (r0 + row) + 1] = tag | __float_as_uint(pl);
+    } else {
+      xh_g[r0 + row] = ph;
+      xl_g[r0 + row] = pl;
+    }
     x[r0 + row] = double(ph) + double(pl);
   }
+  if (xtag) return;
   __syncthreads();
   if (tid == 0) {
     __threadfence();
@@ -1798,7 +1843,7 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
 
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
-              const float* dinv, float* xh, float* xl, const float* dinv128) {
+              const float* dinv, float* xh, float* xl, const float* dinv128, unsigned long long* xtag) {
   const int nblk = int(ceil_div(n, kTB));
   StatScope sc(kStatTrsv, s, double(n) * n, double(n) * n * 0.5 * sizeof(TF));
   UPDES_CUDA_TRY(cudaMemsetAsync(sync_ws, 0, sizeof(int) * (nblk + 2), s));
@@ -1821,11 +1866,18 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
             (e = smem_opt_in((const void*)trsv128_f32_kernel<3>, int(kTrsv128Smem), attr128[3])))
           return e;
         const unsigned g = unsigned(ceil_div(n, kTB2));
+        // UPDES_TRSV_TAGS=0 hands solved blocks over by the finished-block count instead of tagged words
+        static const bool tags_on = [] {
+          const char* v = std::getenv("UPDES_TRSV_TAGS");
+          return !(v && v[0] == '0');
+        }();
+        unsigned long long* tg = tags_on ? xtag : nullptr;
+        if (tg) UPDES_CUDA_TRY(cudaMemsetAsync(tg, 0, 2 * size_t(n) * sizeof(unsigned long long), s));
         switch (mode) {
-          case 0: trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
-          case 1: trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
-          case 2: trsv128_f32_kernel<2><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
-          default: trsv128_f32_kernel<3><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128); break;
+          case 0: trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
+          case 1: trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
+          case 2: trsv128_f32_kernel<2><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
+          default: trsv128_f32_kernel<3><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
         }
         UPDES_LAUNCH_CHECK();
         return UPDES_OK;
@@ -1871,9 +1923,9 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
 }
 
 template int trsv_impl<double>(int, const double*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
-                               const float*, float*, float*, const float*);
+                               const float*, float*, float*, const float*, unsigned long long*);
 template int trsv_impl<float>(int, const float*, int64_t, double*, int, int*, DeviceStatus*, cudaStream_t,
-                              const float*, float*, float*, const float*);
+                              const float*, float*, float*, const float*, unsigned long long*);
 
 namespace {
 

@@ -23,9 +23,12 @@ int lu_factor_impl(int n, double* W, int64_t ldw, TF* F, int64_t ldf, int32_t* p
 // xh, xl (n FP32 each, may be null): scratch planes that carry solved blocks in double-float between CTAs
 // (used together with dinv).
 // dinv128 (with dinv, xh, xl): inverted 128 x 128 diagonal blocks from diag_inverse128, for the 128-row solve.
+// xtag (with dinv128, may be null): 2n 8-byte words through which the 128-row solve hands each solved block
+// to the blocks after it, the double-float value and the block's tag in one word (no flag, no fence).
 template <typename TF>
 int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws, DeviceStatus* st, cudaStream_t s,
-              const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr, const float* dinv128 = nullptr);
+              const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr, const float* dinv128 = nullptr,
+              unsigned long long* xtag = nullptr);
 
 // Inverses of the 64 x 64 diagonal blocks of FP32 LU factors, as double-float planes (diag_inverse_bytes).
 size_t diag_inverse_bytes(int n);

@@ -563,22 +563,22 @@ int factor_core(int n, double* A, int64_t lda, int precision, void* F, int64_t l
 template <typename TF>
 int solve_core(int n, const TF* F, int64_t ldf, const int32_t* piv, double* x, int trans, const LuWs& w,
                cudaStream_t s, const float* dinv = nullptr, float* xh = nullptr, float* xl = nullptr,
-               const float* dinv128 = nullptr) {
+               const float* dinv128 = nullptr, unsigned long long* xtag = nullptr) {
   const int32_t* perm = piv + n;
   const unsigned g = unsigned(ceil_div(n, 256));
   if (!trans) {
     permute_kernel<<<g, 256, 0, s>>>(w.tmp, x, 1, 1, perm, n, 0);
     UPDES_LAUNCH_CHECK();
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv, xh, xl, dinv128);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 0, w.sync, w.st, s, dinv, xh, xl, dinv128, xtag);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv, xh, xl, dinv128);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 1, w.sync, w.st, s, dinv, xh, xl, dinv128, xtag);
     if (e) return e;
     UPDES_CUDA_TRY(cudaMemcpyAsync(x, w.tmp, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
   } else {
     UPDES_CUDA_TRY(cudaMemcpyAsync(w.tmp, x, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv, xh, xl, dinv128);
+    int e = trsv_impl<TF>(n, F, ldf, w.tmp, 2, w.sync, w.st, s, dinv, xh, xl, dinv128, xtag);
     if (e) return e;
-    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv, xh, xl, dinv128);
+    e = trsv_impl<TF>(n, F, ldf, w.tmp, 3, w.sync, w.st, s, dinv, xh, xl, dinv128, xtag);
     if (e) return e;
     permute_kernel<<<g, 256, 0, s>>>(x, w.tmp, 1, 1, perm, n, 1);
     UPDES_LAUNCH_CHECK();
@@ -674,6 +674,7 @@ struct SolveWs {
   float* Wlo;
   float* dinv;     // inverted 64 x 64 diagonal blocks of the FP32 factors (double-float planes)
   float* dinv128;  // the same for 128 x 128 blocks
+  unsigned long long* xtag;  // tagged hand-off words of the 128-row triangular solves (2n)
   int32_t* piv;
   int32_t* state;  // [0] n of the factored system, [1] precision of its factors, [2] 1 when valid
   int64_t ld;
@@ -712,6 +713,7 @@ size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* ou
   w.V = c.take<double>(size_t(m + 1) * n);
   w.partial = c.take<double>(size_t(kDotBlocks) * (m + 2));
   w.h = c.take<double>(m + 2);
+  w.xtag = c.take<unsigned long long>(2 * size_t(n));
   if (out) *out = w;
   return c.off + 256;
 }
@@ -817,7 +819,8 @@ int residual_scaled(const SolveWs& w, int n, const double* x, double* out, doubl
 
 int precond(const SolveWs& w, int n, int precision, double* x, cudaStream_t s, bool trans = false) {
   if (precision == UPDES_PREC_FP64) return solve_core<double>(n, w.W, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s);
-  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv, w.xh, w.xl, w.dinv128);
+  return solve_core<float>(n, w.F32, w.ld, w.piv, x, trans ? 1 : 0, w.lu, s, w.dinv, w.xh, w.xl, w.dinv128,
+                           w.xtag);
 }
 
 [[maybe_unused]] double host_norm(const std::vector<double>& v) {
