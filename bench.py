@@ -315,13 +315,13 @@ def run_ours(args, world, rank, local):
                  "measured_in": "a second pass of the same steps with per-launch CUDA events on each launch's "
                                 "stream (the timed region itself runs without them)"})
     # DRAM bytes (read + write) of the update per algorithmic byte (the double-float C planes read and
-    # written once plus the digit operands), from one ncu capture of the update kernel; applied to this run's
-    # average launch.  An estimate, named with its source.
-    dram_per_alg_byte = {"trailing_update": (1.4777e9 / 1.5008e9,
-                                             "ncu dram__bytes_read.sum + dram__bytes_write.sum of one update "
-                                             "launch at n = 10,006 (m = 9,750, nc = 9,494, K = 256): 1.478 GB "
-                                             "against 1.501 GB algorithmic, scaled by this run's algorithmic "
-                                             "bytes per launch")}
+    # written once plus the digit operands), from one ncu capture of the update kernel at this workload's size;
+    # applied to this run's average launch.  An estimate, named with its source.
+    dram_per_alg_byte = {"trailing_update": (9.2227e9 / 7.8752e9,
+                                             "ncu dram__bytes_read.sum + dram__bytes_write.sum of the largest "
+                                             "update launch at n = 22,506 (m = 22,250, nc = 21,994, K = 256; "
+                                             "UPDES_LOOKAHEAD=0, launch 8): 5.356 + 3.867 GB against 7.875 GB "
+                                             "algorithmic, scaled by this run's algorithmic bytes per launch")}
     if dom in dram_per_alg_byte:
         ratio, src = dram_per_alg_byte[dom]
         roof["traffic"] = ratio * d["bytes"] / d["count"]
