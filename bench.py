@@ -317,10 +317,10 @@ def run_ours(args, world, rank, local):
     # DRAM bytes (read + write) of the update per algorithmic byte (the double-float C planes read and
     # written once plus the digit operands), from one ncu capture of the update kernel at this workload's size;
     # applied to this run's average launch.  An estimate, named with its source.
-    dram_per_alg_byte = {"trailing_update": (9.2227e9 / 7.8752e9,
+    dram_per_alg_byte = {"trailing_update": (8.3175e9 / 7.8752e9,
                                              "ncu dram__bytes_read.sum + dram__bytes_write.sum of the largest "
                                              "update launch at n = 22,506 (m = 22,250, nc = 21,994, K = 256; "
-                                             "UPDES_LOOKAHEAD=0, launch 8): 5.356 + 3.867 GB against 7.875 GB "
+                                             "UPDES_LOOKAHEAD=0, launch 8): 4.458 + 3.859 GB against 7.875 GB "
                                              "algorithmic, scaled by this run's algorithmic bytes per launch")}
     if dom in dram_per_alg_byte:
         ratio, src = dram_per_alg_byte[dom]

@@ -173,28 +173,46 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// 3-D tiled TMA load (x = k offset, y = row, z = digit plane) completing on an mbarrier.
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+// L2 eviction policies for the copies below: the digit tiles of L and U are reused by every tile of their
+// row band / column across the whole launch, while each C tile is read and written once; marking C
+// evict-first and the digits evict-last keeps the streamed C planes (gigabytes per launch at n = 22,506) from
+// pushing the digit tiles out of L2 between their uses.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+// 3-D tiled TMA load (x = k offset, y = row, z = digit plane) completing on an mbarrier, with an L2 policy.
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar,
+                                            uint64_t policy) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
-          "r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3, %4}], [%5], %6;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)), "l"(policy)
       : "memory");
 }
 
-// 2-D tiled TMA load (x = column, y = row) completing on an mbarrier, and the matching bulk-group store.
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+// 2-D tiled TMA load (x = column, y = row) completing on an mbarrier, and the matching bulk-group store, with
+// an L2 policy.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                            uint64_t policy) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-          "r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
       : "memory");
 }
 
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
-  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src, uint64_t policy) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%1, %2}], [%3], %4;" ::"l"(
                    reinterpret_cast<uint64_t>(map)),
-               "r"(x), "r"(y), "r"(src)
+               "r"(x), "r"(y), "r"(src), "l"(policy)
                : "memory");
 }
 
@@ -313,6 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int64_t ncp = int64_t(tiles_n) * TN;  // row stride of the column scales
   const int nkb = Kp / TK;
   volatile int* abort_flag = &ctl.abort_flag;
+  const uint64_t pol_keep = l2_policy_evict_last(), pol_stream = l2_policy_evict_first();
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -363,8 +382,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_expect_tx(&ctl.full[s], uint32_t(kStageBytes));
 #pragma unroll
           for (int p = 0; p < kDigits; ++p) {
-            tma_load_3d(smem_u32(sA + p * kATile), &tmA, kb * TK, r0, p, &ctl.full[s]);
-            tma_load_3d(smem_u32(sB + p * kBTile), &tmB, kb * TK, c0, p, &ctl.full[s]);
+            tma_load_3d(smem_u32(sA + p * kATile), &tmA, kb * TK, r0, p, &ctl.full[s], pol_keep);
+            tma_load_3d(smem_u32(sB + p * kBTile), &tmB, kb * TK, c0, p, &ctl.full[s], pol_keep);
           }
         }
       }
@@ -423,10 +442,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     auto load_c = [&](int t_next, int tl_next) {
       const int r0n = (t_next / tiles_n) * TM, c0n = (t_next % tiles_n) * TN;
       mbar_expect_tx(&ctl.cfull, uint32_t(kCBytes));
-      tma_load_2d(smem_u32(sC), &tmCh, c0n, r0n, &ctl.cfull);
-      tma_load_2d(smem_u32(sC + kCHalf), &tmCh, c0n + 32, r0n, &ctl.cfull);
-      tma_load_2d(smem_u32(sC + 2 * kCHalf), &tmCl, c0n, r0n, &ctl.cfull);
-      tma_load_2d(smem_u32(sC + 3 * kCHalf), &tmCl, c0n + 32, r0n, &ctl.cfull);
+      tma_load_2d(smem_u32(sC), &tmCh, c0n, r0n, &ctl.cfull, pol_stream);
+      tma_load_2d(smem_u32(sC + kCHalf), &tmCh, c0n + 32, r0n, &ctl.cfull, pol_stream);
+      tma_load_2d(smem_u32(sC + 2 * kCHalf), &tmCl, c0n, r0n, &ctl.cfull, pol_stream);
+      tma_load_2d(smem_u32(sC + 3 * kCHalf), &tmCl, c0n + 32, r0n, &ctl.cfull, pol_stream);
       c_pending = tl_next;
     };
     if (storer && blockIdx.x < ntiles) load_c(blockIdx.x, 0);
@@ -536,10 +555,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (storer && !stop) {
         // rows >= m and columns >= nc are outside the tensor and are not written
-        tma_store_2d(&tmCh, c0, r0, smem_u32(sC));
-        tma_store_2d(&tmCh, c0 + 32, r0, smem_u32(sC + kCHalf));
-        tma_store_2d(&tmCl, c0, r0, smem_u32(sC + 2 * kCHalf));
-        tma_store_2d(&tmCl, c0 + 32, r0, smem_u32(sC + 3 * kCHalf));
+        tma_store_2d(&tmCh, c0, r0, smem_u32(sC), pol_stream);
+        tma_store_2d(&tmCh, c0 + 32, r0, smem_u32(sC + kCHalf), pol_stream);
+        tma_store_2d(&tmCl, c0, r0, smem_u32(sC + 2 * kCHalf), pol_stream);
+        tma_store_2d(&tmCl, c0 + 32, r0, smem_u32(sC + 3 * kCHalf), pol_stream);
         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
         asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the buffer has been read
         if (t + int(gridDim.x) < ntiles && !*abort_flag) load_c(t + int(gridDim.x), tl + 1);
