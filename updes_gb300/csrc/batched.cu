@@ -77,6 +77,21 @@ struct OpsF64 {
   static __device__ __forceinline__ double to_d(T a) { return a; }
   static __device__ __forceinline__ void fms(T& c, T a, T b) { c = fma(-a, b, c); }  // c -= a b
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  // acc[a][b] -= sum_k L[a][k] U[k][16 b] over a 4 x 4 register tile (L rows ldl apart, U rows ldu apart)
+  static __device__ __forceinline__ void tile_update(T (&acc)[4][4], const T* L, int ldl, const T* U, int ldu,
+                                                     int kb) {
+    for (int k = 0; k < kb; ++k) {
+      T la[4], ub[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) la[a] = L[a * ldl + k];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) ub[b] = U[k * ldu + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) fms(acc[a][b], la[a], ub[b]);
+    }
+  }
 };
 
 struct OpsDF {
@@ -98,6 +113,59 @@ struct OpsDF {
     c.h = h;
   }
   static __device__ __forceinline__ T mul(T a, T b) { return df_mul(a, b); }
+  // fms on two columns at once with the packed FP32x2 instructions of sm_100+ (one issue slot per pair): the
+  // same operations in the same order as fms, so bitwise the same results; y - x is fma(x, -1, y), which
+  // rounds once like the subtraction
+  static __device__ __forceinline__ float2 sub2(float2 y, float2 x) {
+    return __ffma2_rn(x, make_float2(-1.f, -1.f), y);
+  }
+  static __device__ __forceinline__ void fms2(float2& ch, float2& cl, T a, float2 bh, float2 bl) {
+    const float2 ah = make_float2(a.h, a.h), al = make_float2(a.l, a.l);
+    const float2 p = __fmul2_rn(ah, bh);
+    float2 e = __ffma2_rn(ah, bh, make_float2(-p.x, -p.y));
+    e = __ffma2_rn(ah, bl, __ffma2_rn(al, bh, e));
+    const float2 s = sub2(ch, p);
+    const float2 v = sub2(s, ch);
+    float2 t = sub2(sub2(ch, sub2(s, v)), __fadd2_rn(p, v));
+    t = __fadd2_rn(t, sub2(cl, e));
+    const float2 h = __fadd2_rn(s, t);
+    cl = sub2(t, sub2(h, s));
+    ch = h;
+  }
+  static __device__ __forceinline__ void tile_update(T (&acc)[4][4], const T* L, int ldl, const T* U, int ldu,
+                                                     int kb) {
+    float2 ch[4][2], cl[4][2];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        ch[a][q] = make_float2(acc[a][2 * q].h, acc[a][2 * q + 1].h);
+        cl[a][q] = make_float2(acc[a][2 * q].l, acc[a][2 * q + 1].l);
+      }
+    for (int k = 0; k < kb; ++k) {
+      T la[4];
+      float2 ubh[2], ubl[2];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) la[a] = L[a * ldl + k];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const T u0 = U[k * ldu + 32 * q], u1 = U[k * ldu + 32 * q + 16];
+        ubh[q] = make_float2(u0.h, u1.h);
+        ubl[q] = make_float2(u0.l, u1.l);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) fms2(ch[a][q], cl[a][q], la[a], ubh[q], ubl[q]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        acc[a][2 * q] = {ch[a][q].x, cl[a][q].x};
+        acc[a][2 * q + 1] = {ch[a][q].y, cl[a][q].y};
+      }
+  }
 };
 
 __device__ __forceinline__ double pow2_scale(double m) {
@@ -324,30 +392,22 @@ __device__ int cta_lu(typename Ops::T* W, int64_t ld, int n, int nb, int32_t* pi
           if (c < cols) U[r * kTN + c] = W[int64_t(k0 + r) * ld + c0 + c];
         }
         __syncthreads();
+        // thread (tr, tc) owns rows 4 tr .. 4 tr + 3 and columns tc + 16 b: a warp's loads of a U row are then
+        // 16 consecutive entries (no shared-memory bank conflicts), and its C accesses 128-byte row segments
         T acc[4][4];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const int r = 4 * tr + a, c = 4 * tc + b;
+            const int r = 4 * tr + a, c = tc + 16 * b;
             acc[a][b] = (r < rows && c < cols) ? W[int64_t(r0 + r) * ld + c0 + c] : Ops::from_d(0.0);
           }
-        for (int k = 0; k < kb; ++k) {
-          T la[4], ub[4];
-#pragma unroll
-          for (int a = 0; a < 4; ++a) la[a] = L[(4 * tr + a) * kMaxNB + k];
-#pragma unroll
-          for (int b = 0; b < 4; ++b) ub[b] = U[k * kTN + 4 * tc + b];
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) Ops::fms(acc[a][b], la[a], ub[b]);
-        }
+        Ops::tile_update(acc, L + (4 * tr) * kMaxNB, kMaxNB, U + tc, kTN, kb);
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const int r = 4 * tr + a, c = 4 * tc + b;
+            const int r = 4 * tr + a, c = tc + 16 * b;
             if (r < rows && c < cols) W[int64_t(r0 + r) * ld + c0 + c] = acc[a][b];
           }
       }
