@@ -311,13 +311,17 @@ __global__ void __launch_bounds__(64) trsm_df_kernel(float* Whi, const float* Wl
 
 // U12 = L11^-1 W12 for a full 64-row panel: 64 columns per CTA, 4 lanes per column.  The right-hand sides
 // (double-float planes) are staged in shared memory in one coalesced pass; lane s of a column's group keeps
-// rows s, s+4, ..., s+60 in registers.  Step j (unrolled): the owner of row j rounds it to FP32 (the factor
-// entry), broadcasts it by shuffle, and every lane subtracts L[i][j] * x_j from its rows i > j in
-// double-float arithmetic; the chain is one shuffle per row instead of a 2016-term dependent sum.
+// rows s, s+4, ..., s+60 in registers, as eight pairs (s + 8q, s + 8q + 4) on the packed FP32x2 instructions
+// of sm_100+ (one issue slot per pair; the same operations as scalar code, so bitwise the same results).
+// Step j (unrolled): the owner of row j rounds it to FP32 (the factor entry), broadcasts it by shuffle, and
+// every lane subtracts L[i][j] * x_j from its rows i > j in double-float arithmetic; the chain is one
+// shuffle per row instead of a 2016-term dependent sum.
 struct TrsmDfSmem {
   float L[64][65];
   float Xh[64][65], Xl[64][65];
 };
+
+__device__ __forceinline__ float2 trsm_sub2(float2 y, float2 x) { return __ffma2_rn(x, make_float2(-1.f, -1.f), y); }
 
 __global__ void __launch_bounds__(256) trsm_df64_kernel(float* Whi, const float* Wlo, int64_t ld, int k, int64_t c0,
                                                         int64_t c1) {
@@ -336,32 +340,34 @@ __global__ void __launch_bounds__(256) trsm_df64_kernel(float* Whi, const float*
   __syncthreads();
   const int col = tid >> 2, s = tid & 3;
   const int gbase = lane & ~3;
-  float ah[16], al[16];
+  float2 ah[8], al[8];  // pair q: rows s + 8q (.x) and s + 8q + 4 (.y)
 #pragma unroll
-  for (int r = 0; r < 16; ++r) {
-    ah[r] = sm.Xh[s + 4 * r][col];
-    al[r] = sm.Xl[s + 4 * r][col];
+  for (int q = 0; q < 8; ++q) {
+    ah[q] = make_float2(sm.Xh[s + 8 * q][col], sm.Xh[s + 8 * q + 4][col]);
+    al[q] = make_float2(sm.Xl[s + 8 * q][col], sm.Xl[s + 8 * q + 4][col]);
   }
 #pragma unroll
   for (int j = 0; j < 64; ++j) {
-    // row j lives in slot j / 4 of lane j % 4
-    const float mine = __fadd_rn(ah[j >> 2], al[j >> 2]);
+    // row j lives in slot j / 4 of lane j % 4: pair j / 8, half (j / 4) & 1
+    const int q0 = j >> 3;
+    const float mine = ((j >> 2) & 1) ? __fadd_rn(ah[q0].y, al[q0].y) : __fadd_rn(ah[q0].x, al[q0].x);
     const float xj = __shfl_sync(0xffffffffu, mine, gbase | (j & 3));
     if (s == (j & 3)) sm.Xh[j][col] = xj;
+    const float2 x2 = make_float2(xj, xj);
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-      if (4 * r + 3 <= j) continue;  // every row of this slot is <= j
-      const int i = s + 4 * r;
-      if (i > j) {
-        const float f = -sm.L[i][j];
-        const float p = __fmul_rn(f, xj);
-        const float e = __fmaf_rn(f, xj, -p);
-        const float t0 = __fadd_rn(ah[r], p);
-        const float bb = __fsub_rn(t0, ah[r]);
-        const float tt = __fadd_rn(__fsub_rn(ah[r], __fsub_rn(t0, bb)), __fsub_rn(p, bb));
-        ah[r] = t0;
-        al[r] = __fadd_rn(al[r], __fadd_rn(tt, e));
-      }
+    for (int q = 0; q < 8; ++q) {
+      if (8 * q + 7 <= j) continue;  // both rows of this pair are <= j
+      const int i0 = s + 8 * q, i1 = i0 + 4;
+      const float2 f = make_float2(-sm.L[i0][j], -sm.L[i1][j]);
+      const float2 p = __fmul2_rn(f, x2);
+      const float2 e = __ffma2_rn(f, x2, make_float2(-p.x, -p.y));
+      const float2 t0 = __fadd2_rn(ah[q], p);
+      const float2 bb = trsm_sub2(t0, ah[q]);
+      const float2 tt = __fadd2_rn(trsm_sub2(ah[q], trsm_sub2(t0, bb)), trsm_sub2(p, bb));
+      const float2 nl = __fadd2_rn(al[q], __fadd2_rn(tt, e));
+      // rows i <= j keep their values (only a pair straddling j has one)
+      if (i0 > j) { ah[q].x = t0.x; al[q].x = nl.x; }
+      if (i1 > j) { ah[q].y = t0.y; al[q].y = nl.y; }
     }
   }
   __syncthreads();
