@@ -1736,19 +1736,36 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
   // two accumulators (even and odd columns of a pair) on packed pairs: half the dependent chain and half the
   // instructions
   float2 acc_h = make_float2(0.f, 0.f), acc_l = make_float2(0.f, 0.f);
+  // with xtag, thread tid < 256 reads word tid of each solved block's x two tiles ahead of its use, so that
+  // the blocks solved long before cost no L2 round trip on the way to the last one
+  auto x_word = [&](int q) -> const unsigned long long* {
+    const int c0 = tile_cols(q), rr = tid >> 1;
+    return (tid < 2 * kTB2 && rr < min(kTB2, n - c0)) ? xtag + 2ll * (c0 + rr) + (tid & 1) : nullptr;
+  };
+  unsigned long long wpre[2] = {0ull, 0ull};
+  if (xtag) {
+#pragma unroll
+    for (int d = 0; d < 2; ++d)
+      if (d < t)
+        if (const unsigned long long* p = x_word(d)) wpre[d] = ld_relaxed_u64(p);
+  }
   for (int q = 0; q < t; ++q) {
     const int c0 = tile_cols(q);
     const int cols = min(kTB2, n - c0);
     if (xtag) {
       // tile q is in sT (stored in the previous round, before the barrier that ended it); each of 256
-      // threads waits (bounded) for one word of block q's x
+      // threads takes one word of block q's x, read ahead, and waits (bounded) only if it was not yet there
+      unsigned long long w0 = wpre[0];
+      wpre[0] = wpre[1];
+      if (q + 2 < t)
+        if (const unsigned long long* p = x_word(q + 2)) wpre[1] = ld_relaxed_u64(p);
       if (tid < 2 * kTB2) {
         const int rr = tid >> 1;
         float v = 0.f;
         if (rr < cols) {
           const unsigned want = unsigned(c0 / kTB2 + 1);
           const unsigned long long* p = xtag + 2ll * (c0 + rr) + (tid & 1);
-          unsigned long long w = ld_relaxed_u64(p);
+          unsigned long long w = w0;
           long long it = 0;
           while (unsigned(w >> 32) != want) {
             if (++it > spin_limit()) {
