@@ -39,7 +39,7 @@ namespace {
 
 constexpr int TM = 128, TN = 64, TK = 64;
 constexpr int kDigits = 3, kGroups = 4;  // 8 digit products
-constexpr int kStages = 2;
+constexpr int kStages = 2;  // equal to the number of accumulator sets (one barrier serves both)
 // epilogue: kEpiWarps warps, four per lane quarter of the tile (the warps a TMEM lane quarter allows), each
 // with kEpiCols columns
 constexpr int kEpiWarps = 16, kEpiCols = TN / (kEpiWarps / 4);
@@ -310,7 +310,9 @@ __global__ void __launch_bounds__(256) digits_kernel(const float* __restrict__ A
 
 // ---- main kernel ---------------------------------------------------------------------------------------
 struct Ctrl {
-  uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], cfull, cready;
+  // With two stages and two accumulator sets, k block j uses stage j % 2 and set j % 2: the one commit of its
+  // MMAs (tfull[j % 2]) both hands the set to the epilogue and frees the stage for the producer.
+  uint64_t full[kStages], tfull[2], tempty[2], cfull, cready;
   uint32_t tmem;
   int abort_flag;
 };
@@ -336,7 +338,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&ctl.full[s], 1);
-      mbar_init(&ctl.empty[s], 1);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&ctl.tfull[s], 1);
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int kb = 0; kb < nkb; ++kb, ++j) {
           const int s = j % kStages;
           const uint32_t ph = uint32_t(j / kStages) & 1u;
-          if (!mbar_wait(&ctl.empty[s], ph ^ 1u, abort_flag)) {
+          if (!mbar_wait(&ctl.tfull[s], ph ^ 1u, abort_flag)) {  // k block j - 2's MMAs are done
             if (!*abort_flag) { status_error(st, UPDES_ERR_TIMEOUT); atomicCAS(&st->timeout_tag, 0, 41); }
             *abort_flag = 1;
             break;
@@ -422,7 +423,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           mma_product<2, 0>(tset, a0, b0);
           mma_product<1, 2>(tset, a0, b0);
           mma_product<2, 1>(tset, a0, b0);
-          mma_commit(&ctl.empty[s]);
           mma_commit(&ctl.tfull[set]);
           last_commit = j;
         }
