@@ -666,7 +666,7 @@ namespace {
 
 struct SolveWs {
   LuWs lu;
-  double *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *partial, *h;
+  double *W, *dr, *dc, *bs, *bsabs, *absr, *x, *r, *z, *wv, *V, *Z, *partial, *h;
   double* evp;  // per-tile partial sums of the symmetric value evaluation
   float *Khi, *Klo;  // equilibrated K as double-float planes (kept for the refinement's residuals)
   float *xh, *xl;    // FP32 planes of the vector a GEMV multiplies
@@ -714,6 +714,7 @@ size_t solve_ws_layout(int n, const updes_solve_opts& o, char* base, SolveWs* ou
   w.partial = c.take<double>(size_t(kDotBlocks) * (m + 2));
   w.h = c.take<double>(m + 2);
   w.xtag = c.take<unsigned long long>(2 * size_t(n));
+  w.Z = c.take<double>(size_t(m) * n);  // preconditioned basis vectors M^-1 V_j of a restart cycle
   if (out) *out = w;
   return c.off + 256;
 }
@@ -838,7 +839,8 @@ bool trace_on() {
   return on;
 }
 
-// Restarted, right-preconditioned GMRES on Ks x = bs starting from w.x.
+// Restarted, right-preconditioned GMRES on Ks x = bs starting from w.x, in the flexible form: each cycle keeps
+// its preconditioned vectors, so that its update x += M^-1 V y is Z y without another preconditioner solve.
 int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, updes_solve_info* info,
           cudaStream_t s, bool trans = false) {
   const int m = o.restart;
@@ -884,10 +886,12 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
     gv[0] = beta;
     int j = 0;
     for (; j < m && total < o.max_iters; ++j, ++total) {
+      // z_j = M^-1 v_j is kept (flexible GMRES form): the cycle's update is then Z y, with no further solve
       double* vj = w.V + size_t(j) * n;
-      UPDES_CUDA_TRY(cudaMemcpyAsync(w.z, vj, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
-      if ((e = precond(w, n, precision, w.z, s, trans))) return e;
-      if ((e = apply_K(w, n, w.z, w.wv, s, trans))) return e;
+      double* zj = w.Z + size_t(j) * n;
+      UPDES_CUDA_TRY(cudaMemcpyAsync(zj, vj, size_t(n) * 8, cudaMemcpyDeviceToDevice, s));
+      if ((e = precond(w, n, precision, zj, s, trans))) return e;
+      if ((e = apply_K(w, n, zj, w.wv, s, trans))) return e;
       // CGS2
       std::fill(hcol.begin(), hcol.end(), 0.0);
       for (int pass = 0; pass < 2; ++pass) {
@@ -936,9 +940,8 @@ int gmres(const SolveWs& w, int n, int precision, const updes_solve_opts& o, upd
     }
     if (j > 0) {
       UPDES_CUDA_TRY(cudaMemcpyAsync(w.h, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, s));
-      multi_axpy_kernel<<<g, 256, 0, s>>>(w.V, n, j, w.h, 1.0, nullptr, w.z, n);
+      multi_axpy_kernel<<<g, 256, 0, s>>>(w.Z, n, j, w.h, 1.0, nullptr, w.z, n);
       UPDES_LAUNCH_CHECK();
-      if ((e = precond(w, n, precision, w.z, s, trans))) return e;
       axpby_kernel<<<g, 256, 0, s>>>(w.x, 1.0, w.z, 1.0, n, nullptr);
       UPDES_LAUNCH_CHECK();
       UPDES_CUDA_TRY(cudaStreamSynchronize(s));
