@@ -334,9 +334,9 @@ constexpr int kDotBlocks = 120;
 // from the double-float planes of K (48 significant bits per entry), which by themselves put the
 // measured backward error of an FP64 LU solution at roughly 50-100 unit roundoffs.
 constexpr double kBwdFloor = 256.0 * 1.1102230246251565e-16;
-// A restart cycle stops its inner iteration once the estimated residual has fallen by this factor: the
-// update it then applies goes through the FP32 factors, whose solves are accurate to about 1e-6 of the
-// correction, so the true residual cannot follow the estimate further within one cycle.
+// A restart cycle stops its inner iteration once the estimated residual has fallen by this factor, or earlier
+// at the requested tolerance or at the reduction that brings the backward error to its floor (at N = 22,500
+// the floor comes first and one cycle of 10 iterations converges; 1e-10 and 1e-14 here measured the same).
 constexpr double kInnerReduction = 1e-6;
 
 // partial[b * nv + i] = sum over block b's chunk of V_i . w
