@@ -30,8 +30,9 @@ import os
 import threading
 
 from . import _lib
-from .operators import (DEFAULT_OPTIONS, CollocationMatrix, DeviceProblem, SteadySol, _torch,
-                        boundary_conditions_func_to_arr, materialize_B, prepare)
+from .operators import (DEFAULT_OPTIONS, CollocationMatrix, SteadySol, _torch, boundary_conditions_func_to_arr,
+                        compute_nb_monomials, materialize_B, prepare)
+from .rbf import rbf_spec
 
 PANEL_CANDIDATES = (16, 32, 64)
 SIZE_BUCKETS = (256, 512, 1024, 2048, 4096)
@@ -114,22 +115,97 @@ def default_tuner() -> PanelTuner:
     return _TUNER
 
 
-class _Batch:
-    """Device arrays and C structs of one batch (kept alive while the library uses them)."""
+def _align(k: int, unit: int) -> int:
+    return (k + unit - 1) // unit * unit
 
-    def __init__(self, dps, qs):
+
+class _PackedProblem:
+    """One system of a batch: sizes, kernel and the ``updes_problem`` struct, whose arrays live in the batch's
+    packed device buffers (the object keeps them alive)."""
+
+    def __init__(self, cloud, rbf, max_degree, device, keep):
+        self.torch = _torch()
+        self.device = device
+        self.N, self.Ni = cloud.N, cloud.Ni
+        self.M = compute_nb_monomials(max_degree)
+        self.n = self.N + self.M
+        self.kid, self.param = rbf_spec(rbf)
+        self.keep = keep
+        self.c = _lib.Problem()
+
+    def stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+
+class _Batch:
+    """Every system's arrays packed into a few device buffers (one host-to-device copy per element type), the
+    C structs pointing into them, and one output buffer for all coefficients and values."""
+
+    def __init__(self, clouds, rbfs, degrees, prepared, self_term):
+        import numpy as np
         torch = _torch()
         self.torch = torch
-        self.dps, self.qs = dps, qs
-        self.count = len(dps)
-        dev = dps[0].device
-        self.coeffs = [torch.empty(dp.n, dtype=torch.float64, device=dev) for dp in dps]
-        self.vals = [torch.empty(dp.N, dtype=torch.float64, device=dev) for dp in dps]
-        c = self.count
-        self.probs = (_lib.Problem * c)(*[dp.c for dp in dps])
-        ptrs = lambda ts: (ctypes.c_void_p * c)(*[t.data_ptr() for t in ts])
-        self.qp, self.cp, self.vp = ptrs(qs), ptrs(self.coeffs), ptrs(self.vals)
+        dev = torch.device("cuda", torch.cuda.current_device())
+        c = len(prepared)
+        self.count = c
+        # offsets (in elements) of each system's arrays: 32 doubles / 64 ints = 256 bytes
+        f_off, i_off, o_off = [], [], []
+        fpos = ipos = opos = 0
+        for cl, (W, kind, bnodes, geom, q), deg in zip(clouds, prepared, degrees):
+            N, Ni, Nb = cl.N, cl.Ni, cl.N - cl.Ni
+            n = N + compute_nb_monomials(deg)
+            sizes = (2 * N, 5 * Ni, 8 * Nb, N)  # nodes, op weights, boundary geometry, q
+            offs = []
+            for sz in sizes:
+                offs.append(fpos)
+                fpos = _align(fpos + sz, 32)
+            f_off.append(offs)
+            i_off.append((ipos, _align(ipos + Nb, 64)))  # boundary kinds, boundary node pairs
+            ipos = _align(i_off[-1][1] + 2 * Nb, 64)
+            o_off.append((opos, _align(opos + n, 32)))  # coefficients, values
+            opos = _align(o_off[-1][1] + N, 32)
+        fh = np.zeros(max(fpos, 1), dtype=np.float64)
+        ih = np.zeros(max(ipos, 1), dtype=np.int32)
+        for cl, (W, kind, bnodes, geom, q), fo, io in zip(clouds, prepared, f_off, i_off):
+            N, Ni, Nb = cl.N, cl.Ni, cl.N - cl.Ni
+            fh[fo[0]:fo[0] + 2 * N] = np.asarray(cl.sorted_nodes, dtype=np.float64).ravel()
+            fh[fo[1]:fo[1] + 5 * Ni] = np.asarray(W, dtype=np.float64).ravel()
+            fh[fo[2]:fo[2] + 8 * Nb] = np.asarray(geom, dtype=np.float64).ravel()
+            fh[fo[3]:fo[3] + N] = np.asarray(q, dtype=np.float64)
+            ih[io[0]:io[0] + Nb] = np.asarray(kind, dtype=np.int32)
+            ih[io[1]:io[1] + 2 * Nb] = np.asarray(bnodes, dtype=np.int32).ravel()
+        self.fbuf = torch.from_numpy(fh).to(dev)
+        self.ibuf = torch.from_numpy(ih).to(dev)
+        self.obuf = torch.empty(max(opos, 1), dtype=torch.float64, device=dev)
+        fb, ib, ob = self.fbuf.data_ptr(), self.ibuf.data_ptr(), self.obuf.data_ptr()
+        keep = (self.fbuf, self.ibuf)
+        self.dps = []
+        qv, cv, vv = [], [], []
+        for cl, rbf, deg, fo, io, oo in zip(clouds, rbfs, degrees, f_off, i_off, o_off):
+            dp = _PackedProblem(cl, rbf, deg, dev, keep)
+            p = dp.c
+            p.N, p.Ni, p.M, p.rbf, p.rbf_param = dp.N, dp.Ni, dp.M, dp.kid, dp.param
+            p.self_term = int(bool(self_term))
+            p.nodes = fb + 8 * fo[0]
+            p.op_weights = fb + 8 * fo[1] if dp.Ni else None
+            has_bd = dp.N > dp.Ni
+            p.bd_kind = ib + 4 * io[0] if has_bd else None
+            p.bd_node = ib + 4 * io[1] if has_bd else None
+            p.bd_geom = fb + 8 * fo[2] if has_bd else None
+            self.dps.append(dp)
+            qv.append(fb + 8 * fo[3])
+            cv.append(ob + 8 * oo[0])
+            vv.append(ob + 8 * oo[1])
+        self.o_off = o_off
+        self.probs = (_lib.Problem * c)(*[dp.c for dp in self.dps])
+        ptrs = lambda vs: (ctypes.c_void_p * c)(*vs)
+        self.qp, self.cp, self.vp = ptrs(qv), ptrs(cv), ptrs(vv)
         self.infos = (_lib.SolveInfo * c)()
+
+    def results(self):
+        """(coeffs, vals) of every system as host arrays, from one device-to-host copy."""
+        host = self.obuf.cpu().numpy()
+        return [(host[co:co + dp.n].copy(), host[vo:vo + dp.N].copy()) for dp, (co, vo) in zip(self.dps, self.o_off)]
 
     def run(self, idx, precisions, widths, max_sweeps, ctas):
         """Solve the systems ``idx`` (host indices into the batch) in one launch; returns the status."""
@@ -213,20 +289,23 @@ def pde_solver_batched(systems, options=None, precision="auto", max_sweeps=4, ct
     torch = _torch()
     opts = options or DEFAULT_OPTIONS
     t0 = time.perf_counter()
-    dps, qs = [], []
+    prepared = []
     for sysd in systems:
         cloud = sysd["cloud"]
+        n = cloud.N + compute_nb_monomials(sysd["max_degree"])
+        if n > MAX_N:
+            raise ValueError(f"system of n = {n} unknowns exceeds the batched solver's limit of {MAX_N}")
         bcs = boundary_conditions_func_to_arr(sysd["boundary_conditions"], cloud)
-        W, kind, bnodes, geom, q = prepare(sysd["diff_operator"], sysd["rhs_operator"], cloud, bcs, sysd["rbf"],
-                                           sysd["max_degree"], sysd.get("diff_args"), sysd.get("rhs_args"), opts)
-        dp = DeviceProblem(cloud, sysd["rbf"], sysd["max_degree"], W, kind, bnodes, geom, opts.self_term)
-        if dp.n > MAX_N:
-            raise ValueError(f"system of n = {dp.n} unknowns exceeds the batched solver's limit of {MAX_N}")
-        dps.append(dp)
-        qs.append(torch.as_tensor(q, dtype=torch.float64, device=dp.device))
-    if not dps:
+        prepared.append(prepare(sysd["diff_operator"], sysd["rhs_operator"], cloud, bcs, sysd["rbf"],
+                                sysd["max_degree"], sysd.get("diff_args"), sysd.get("rhs_args"), opts))
+    if not prepared:
         return []
-    batch = _Batch(dps, qs)
+    for sysd in systems:
+        if getattr(sysd["cloud"], "sorted_local_supports", None) is not None:
+            raise _lib.UpdesError(_lib.ERR_UNSUPPORTED, "updes_solve_batched (local supports)")
+    batch = _Batch([s["cloud"] for s in systems], [s["rbf"] for s in systems], [s["max_degree"] for s in systems],
+                   prepared, opts.self_term)
+    dps = batch.dps
     names = precision if isinstance(precision, (list, tuple)) else [precision] * len(dps)
     code = {"fp32": _lib.PREC_FP32, "auto": _lib.PREC_FP32, "fp64": _lib.PREC_FP64}
     precs = [code[p] for p in names]
@@ -260,9 +339,8 @@ def pde_solver_batched(systems, options=None, precision="auto", max_sweeps=4, ct
                             for i in range(len(dps))]
     _lib.check(st, "updes_solve_batched")
     out = []
-    for sysd, dp, c, v in zip(systems, dps, batch.coeffs, batch.vals):
+    for sysd, dp, (c, v) in zip(systems, dps, batch.results()):
         cloud, rbf, deg = sysd["cloud"], sysd["rbf"], sysd["max_degree"]
-        out.append(SteadySol(v.cpu().numpy(), c.cpu().numpy(),
-                             CollocationMatrix(lambda dp=dp, cloud=cloud, rbf=rbf, deg=deg:
-                                               materialize_B(dp, cloud, rbf, deg))))
+        out.append(SteadySol(v, c, CollocationMatrix(lambda dp=dp, cloud=cloud, rbf=rbf, deg=deg:
+                                                     materialize_B(dp, cloud, rbf, deg))))
     return out
