@@ -244,3 +244,26 @@ def multi_initial(case, nodes):
 GMSH_CASE = dict(mesh="dshape.msh", facets={"Bottom": "d", "Right": "n", "Top": "r", "Left": "d"},
                  rbf=("polyharmonic", 1), max_degree=1, op="laplacian",
                  bc={"Bottom": "sinsin", "Right": "xy", "Top": ("ylin", "beta2"), "Left": "zero"}, rhs="poisson_rhs")
+
+
+# Field helpers around the solve (updes/operators.py:190-208, 211-291, 354-371, 381-509).  The integral
+# case is the reference's own unit test problem (updes/tests/test_integrals.py: 12 x 12 Dirichlet cloud,
+# r^11 (polyharmonic a = 5), degree 3, s = x^2 / (1 + y^2), whose integral over the unit square is pi/12),
+# plus a 12 x 9 jittered cloud on which the reference's quadrature points are not the cell centres; the
+# interpolation case is its test_interpolation.py problem (8 x 8, two facet assignments, field = node id).
+FIELD_INTEGRAL_CASES = {
+    "integral_12x12": dict(Nx=12, Ny=12, facets=dict(North="d", South="d", East="d", West="d"), jitter=None,
+                           rbf=("polyharmonic", 5), max_degree=3),
+    "integral_12x9_jitter": dict(Nx=12, Ny=9, facets=dict(North="d", South="n", East="d", West="r"),
+                                 jitter=(0.2, 41), rbf=("polyharmonic", 5), max_degree=3),
+}
+FIELD_INTERP_CASE = dict(Nx=8, Ny=8, facets1=dict(South="n", West="d", North="n", East="d"),
+                         facets2=dict(South="d", West="n", North="d", East="n"))
+FIELD_FD_CASE = dict(Nx=9, Ny=7, facets=dict(North="n", South="n", East="d", West="n"), jitter=(0.15, 7))
+FIELD_EVAL_POINTS = np.array([[0.31, 0.42], [0.5, 0.5], [0.05, 0.9], [0.77, 0.13], [1.0, 0.25], [0.0, 0.0],
+                              [0.62, 0.99]])
+
+
+def field_s(X):
+    """s = x^2 / (1 + y^2) (updes/tests/test_integrals.py)."""
+    return X[:, 0] ** 2 / (1 + X[:, 1] ** 2)

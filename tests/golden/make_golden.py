@@ -12,7 +12,9 @@ outputs in ``tests/golden/<case>.npz``.  It also differentiates the reference
 solve (reverse mode, through inv/GEMM/QR) for the boundary-control adjoint case,
 runs the reference's ``pde_multi_solver`` on the two-field cases of
 ``cases.MULTI_CASES``, and reads the synthetic mesh of ``make_msh.py`` with the
-reference's ``GmshCloud`` (solving ``cases.GMSH_CASE`` on it).
+reference's ``GmshCloud`` (solving ``cases.GMSH_CASE`` on it), and runs the reference's field helpers
+(``integrate_field``, ``interpolate_field``, ``gradient_vals_vec``, the grid finite differences) on the
+``cases.FIELD_*`` problems.
 """
 from __future__ import annotations
 
@@ -297,13 +299,69 @@ def run_ref_fixture(updes, ref_path):
           f"max |div| {np.abs(divs).max():.2e} {time.time() - t0:.1f}s")
 
 
+def run_fields(updes):
+    """Field helpers: the reference's integrate_field on coefficients from its own interpolation solve,
+    gradient_vals_vec / laplacian_vals_vec at a few points, interpolate_field between two numberings of one
+    grid, apply_neumann_conditions, cartesian_gradient_vec and enforce_cartesian_gradient_neumann on a
+    jittered grid with Neumann facets.  Writes tests/golden/fields_helpers.npz."""
+    import jax.numpy as jnp
+    t0 = time.time()
+    npy = lambda t: np.asarray(t.detach() if isinstance(t, torch.Tensor) else t, dtype=np.float64)
+    out = {}
+
+    def injected(Nx, Ny, facets, coords, support="max"):
+        class InjectedCloud(updes.SquareCloud):
+            def define_node_coordinates(self, noise_key):
+                self.nodes = {g: torch.tensor(coords[g]) for g in range(self.N)}
+        return InjectedCloud(Nx=Nx, Ny=Ny, facet_types=dict(facets), support_size=support)
+
+    for name, fc in C.FIELD_INTEGRAL_CASES.items():
+        coords = C.grid_coords(fc)
+        cloud = injected(fc["Nx"], fc["Ny"], fc["facets"], coords)
+        rbf = partial(updes.polyharmonic, a=int(fc["rbf"][1]))
+        X = npy(cloud.sorted_nodes)
+        s = C.field_s(X)
+        coeffs = updes.get_field_coefficients(jnp.asarray(s), cloud, rbf, fc["max_degree"])
+        val = updes.integrate_field(coeffs, cloud, rbf, fc["max_degree"])
+        P = jnp.asarray(C.FIELD_EVAL_POINTS)
+        gv = updes.gradient_vals_vec(P, jnp.asarray(s), cloud, rbf, fc["max_degree"])
+        lv = updes.laplacian_vals_vec(P, jnp.asarray(s), cloud, rbf, fc["max_degree"])
+        out.update({f"{name}_field": s, f"{name}_coeffs": npy(coeffs), f"{name}_integral": np.float64(npy(val)),
+                    f"{name}_gradient_vals": npy(gv), f"{name}_laplacian_vals": npy(lv),
+                    f"{name}_sorted_nodes": X})
+        print(f"{name}: integral {float(npy(val)):.12f} (pi/12 = {np.pi / 12:.12f})")
+
+    ic = C.FIELD_INTERP_CASE
+    N = ic["Nx"] * ic["Ny"]
+    c1 = updes.SquareCloud(Nx=ic["Nx"], Ny=ic["Ny"], facet_types=dict(ic["facets1"]), support_size=N - 1)
+    c2 = updes.SquareCloud(Nx=ic["Nx"], Ny=ic["Ny"], facet_types=dict(ic["facets2"]), support_size=N - 1)
+    field = jnp.arange(0, c1.N)
+    out["interp_field"] = npy(field)
+    out["interp_result"] = npy(updes.interpolate_field(field, c1, c2))
+
+    fd = C.FIELD_FD_CASE
+    coords = C.grid_coords(fd)
+    cloud = injected(fd["Nx"], fd["Ny"], fd["facets"], coords)
+    X = npy(cloud.sorted_nodes)
+    f = np.sin(2.0 * X[:, 0]) + X[:, 1] ** 2 + 0.3 * X[:, 0] * X[:, 1]
+    bcs = {k: None for k in fd["facets"]}
+    out["fd_field"] = f
+    out["fd_sorted_nodes"] = X
+    out["fd_neumann"] = npy(updes.apply_neumann_conditions(jnp.asarray(f), bcs, cloud))
+    grads = updes.cartesian_gradient_vec(range(cloud.N), jnp.asarray(f), cloud)
+    out["fd_cartesian_gradient"] = npy(grads)
+    out["fd_enforced"] = npy(updes.enforce_cartesian_gradient_neumann(jnp.asarray(f), grads, bcs, cloud))
+    np.savez_compressed(os.path.join(HERE, "fields_helpers.npz"), **out)
+    print(f"fields_helpers: {len(out)} arrays, {time.time() - t0:.1f}s")
+
+
 if __name__ == "__main__":
     if len(sys.argv) < 2:
         sys.exit("usage: make_golden.py <path of the Updes source tree> [case ...]")
     ref = sys.argv[1]
     updes = load_reference(ref)
     only = sys.argv[2:] or (list(C.CASES) + list(C.MULTI_CASES) + list(C.LOCAL_CASES)
-                            + ["gmsh", "ref_fixture", "adjoint_local"])
+                            + ["gmsh", "ref_fixture", "adjoint_local", "fields"])
     for name in only:
         if name == "adjoint":
             continue
@@ -312,6 +370,9 @@ if __name__ == "__main__":
             continue
         if name == "ref_fixture":
             run_ref_fixture(updes, ref)
+            continue
+        if name == "fields":
+            run_fields(updes)
             continue
         if name == "adjoint_local":
             run_adjoint(updes, C.LOCAL_ADJOINT_CASE)
