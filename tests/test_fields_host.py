@@ -55,3 +55,25 @@ def test_grid_finite_differences_match_the_reference():
     nm = np.concatenate([cloud.facet_nodes[k] for k, t in fd["facets"].items() if t == "n"])
     other = np.setdiff1d(np.arange(cloud.N), nm)
     assert np.array_equal(enf[other], grads[other])
+
+
+def test_small_helpers():
+    a = np.arange(6.0).reshape(3, 2)
+    b = np.ones((3, 2))
+    assert np.array_equal(F.dot_vec(a, b), a.sum(axis=1))
+    J = np.arange(12.0).reshape(3, 2, 2)
+    assert np.array_equal(F.dot_mat(J, b), J.sum(axis=2))
+    cl = SquareCloud(Nx=6, Ny=5, facet_types=dict(North="pn", South="pn", East="d", West="r"))
+    bcs = {"North": np.ones(len(cl.facet_nodes["North"])), "South": 3.0, "East": 1.0,
+           "West": (2.0, lambda x: 0.5 + x[1])}
+    z = F.zerofy_periodic_cond(dict(bcs), cl)
+    assert np.array_equal(z["North"], np.zeros(len(cl.facet_nodes["North"])))
+    robin, vals = F.duplicate_robin_coeffs(bcs, cl)
+    assert vals["West"] == 2.0 and vals["East"] == 1.0
+    W = np.asarray(cl.facet_nodes["West"])
+    assert sorted(robin) == sorted(int(i) for i in W)
+    assert np.allclose([robin[int(i)] for i in W], 0.5 + cl.sorted_nodes[W, 1])
+    # the solver's own Robin rows use the same coefficients
+    from updes_gb300.operators import _bc_values_and_betas
+    _, robin_solver = _bc_values_and_betas(bcs, cl, True)
+    assert robin_solver == robin

@@ -59,3 +59,13 @@ def test_gradient_and_laplacian_of_nodal_values_match_the_reference(name):
     assert np.allclose(one, g[0], rtol=1e-12, atol=1e-12)
     one_l = F.laplacian_vals(C.FIELD_EVAL_POINTS[0], s, cloud, rbf, fc["max_degree"])
     assert abs(one_l - lap[0]) <= 1e-12 * max(1.0, abs(lap[0]))
+
+
+def test_divergence_vec_is_the_sum_of_the_columns_gradients():
+    name = "integral_12x9_jitter"
+    fc, cloud, rbf = _setup(name)
+    c = GOLD[f"{name}_coeffs"]
+    c2 = np.stack([c, 2.0 * c], axis=-1)
+    d = F.divergence_vec(C.FIELD_EVAL_POINTS, c2, cloud.sorted_nodes, rbf)
+    g = U.gradient_vec(C.FIELD_EVAL_POINTS, c, cloud.sorted_nodes, rbf)
+    assert np.allclose(d, g[:, 0] + 2.0 * g[:, 1], rtol=1e-13, atol=1e-13)

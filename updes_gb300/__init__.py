@@ -14,9 +14,10 @@ from .operators import (
     pde_solver_many, pde_solver_jit_with_bc, value, value_vec,
 )
 from .batched import PanelTuner, pde_solver_batched
-from .fields import (apply_neumann_conditions, cartesian_gradient, cartesian_gradient_vec,
-                     enforce_cartesian_gradient_neumann, gradient_vals, gradient_vals_vec, integrate_field,
-                     interpolate_field, laplacian_vals, laplacian_vals_vec)
+from .fields import (apply_neumann_conditions, cartesian_gradient, cartesian_gradient_vec, divergence_vec, dot_mat,
+                     dot_vec, duplicate_robin_coeffs, enforce_cartesian_gradient_neumann, gradient_vals,
+                     gradient_vals_vec, integrate_field, interpolate_field, laplacian_vals, laplacian_vals_vec,
+                     zerofy_periodic_cond)
 from .rbf import distance, gaussian, inverse_multiquadric, multiquadric, polyharmonic, rbf_spec, thin_plate
 
 __version__ = "0.1.0"

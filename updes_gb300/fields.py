@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .operators import compute_nb_monomials, core_compute_coefficients, gradient, laplacian, value, value_vec
+from .operators import compute_nb_monomials, core_compute_coefficients, gradient, laplacian, value_vec
 
 
 def gradient_vals(x, field, cloud, rbf, max_degree):
@@ -171,3 +171,55 @@ def enforce_cartesian_gradient_neumann(field, grads, boundary_conditions, cloud,
             j, dist, _ = _opposite_closest(cloud, i, cloud.outward_normals[i])
             out[i] = (field[i] - field[j]) / dist
     return np.clip(out, -clip_val, clip_val) if clip_val else out
+
+
+def divergence_vec(xs, field, centers, rbf=None):
+    """``divergence`` at the rows of xs (m, 2) of a vector field given by its two coefficient columns
+    (updes/operators.py:314)."""
+    from .operators import divergence
+    return divergence(np.asarray(xs, dtype=np.float64).reshape(-1, 2), field, centers, rbf)
+
+
+def dot_vec(a, b):
+    """Row-wise dot products of two (m, d) arrays (updes/operators.py:778)."""
+    return np.einsum("ij,ij->i", np.asarray(a), np.asarray(b))
+
+
+def dot_mat(J, v):
+    """Row-wise matrix-vector products J[i] @ v[i] of (m, p, d) and (m, d) arrays (updes/operators.py:779)."""
+    return np.einsum("ipd,id->ip", np.asarray(J), np.asarray(v))
+
+
+def zerofy_periodic_cond(boundary_conditions, cloud):
+    """Zero values on the periodic facets, in place, as the solve does before it runs
+    (updes/operators.py:546-555)."""
+    for f, t in cloud.facet_types.items():
+        if t[0] == "p":
+            boundary_conditions[f] = np.zeros(len(cloud.facet_nodes[f]))
+    return boundary_conditions
+
+
+def duplicate_robin_coeffs(boundary_conditions, cloud):
+    """(Robin coefficient per node, the boundary conditions with the Robin facets' values alone)
+    (updes/operators.py:512-541).  A Robin facet given as (values, betas) spreads betas (an array, or a
+    callable evaluated on the facet's nodes) over its nodes by position i - first node id, as the reference
+    does, with the index clamped to the facet as the solver's compatibility mode does; a facet given without
+    betas gets zeros."""
+    from .operators import _eval_on_nodes
+    robin, out = {}, {}
+    for f, t in cloud.facet_types.items():
+        bc = boundary_conditions[f]
+        if t != "r":
+            out[f] = bc
+            continue
+        ids = cloud.facet_nodes[f]
+        if isinstance(bc, tuple):
+            out[f], betas = bc[0], bc[1]
+            if callable(betas):
+                betas = _eval_on_nodes(betas, cloud.sorted_nodes[np.asarray(ids, dtype=np.int64)])
+        else:
+            out[f], betas = bc, np.zeros(len(ids))
+        betas = np.broadcast_to(np.asarray(betas, dtype=np.float64), (len(ids),))
+        for i in ids:
+            robin[i] = float(betas[min(max(i - ids[0], 0), len(ids) - 1)])
+    return robin, out
