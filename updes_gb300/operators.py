@@ -206,6 +206,7 @@ def _probing(state):
 
 
 _BASIS = [dict(value=1.0), dict(gx=1.0), dict(gy=1.0), dict(lap=1.0), dict(hxx=1.0), dict(hyy=1.0)]
+_STACKED_PROBE_MAX_NODES = 2048
 
 
 def capture_operator(diff_operator, X, rbf, fields):
@@ -243,6 +244,10 @@ def capture_operator(diff_operator, X, rbf, fields):
         # All eight probes (zero, the six unit primitives, the random check) in one call: each primitive
         # returns a column of its eight probe values, which broadcasts against the (m,) node arrays into an
         # (8, m) result.  Kept only when its random-check row equals a separate evaluation of that probe.
+        # It saves call overhead on small clouds; on large ones the (8, m) temporaries cost more than the
+        # seven calls they replace (0.83 against 0.70 ms at m = 3,969), so those probe one by one.
+        if m > _STACKED_PROBE_MAX_NODES:
+            raise ValueError("large cloud")
         lanes = np.zeros((8, 6))
         lanes[1:7] = np.eye(6)
         lanes[7] = rv
