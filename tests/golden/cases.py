@@ -99,7 +99,7 @@ def make_rhs_field(case, nodes):
 
 
 CASES = {
-    # the README example (configs[0]): Laplace, S=Neumann, W/E/N Dirichlet, r^3, degree 1
+    # the reference README example: Laplace, S=Neumann, W/E/N Dirichlet, r^3, degree 1
     "readme_laplace_30x20": dict(Nx=30, Ny=20, facets={"South": "n", "West": "d", "North": "d", "East": "d"},
                                  rbf=("polyharmonic", 1), max_degree=1, jitter=None, op="laplacian",
                                  bc={"South": "zero", "West": "zero", "North": "sinpix", "East": "zero"},
