@@ -1659,7 +1659,9 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
 // go to xtag[2i] and xtag[2i + 1] as (block + 1) << 32 | float bits, each one single-copy-atomic 8-byte store,
 // so a reader that sees its block's tag has the value, with no flag, no fence and no second round trip.  The
 // words are cleared before every call, so a tag can only come from the current call.
-template <int MODE>
+// VEC (untransposed modes, factors 16-byte aligned with a row stride of whole 16-byte vectors): tiles move as
+// 16-byte vectors.
+template <int MODE, bool VEC = false>
 __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restrict__ F, int64_t ldf, int n, double* x,
                                                           float* xh_g, float* xl_g, int* ticket, int* flags,
                                                           DeviceStatus* st, const float* __restrict__ dinv128,
@@ -1703,7 +1705,32 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
       sDl[ra][cb] = __ldg(Dlo + e);
     }
   }
+  // Untransposed tiles of 16-byte aligned factors move as 16-byte vectors: a thread's eight loads per tile
+  // (rows 4 (w >> 2) + (j >> 3), columns 32 (w & 3) + 4 (j & 7) for chunk w, lane j: a warp reads four
+  // 128-byte row segments) keep four times fewer requests in flight than 4-byte loads, which bounded the
+  // tile stream.  Other tiles move as 4-byte loads.
+  constexpr bool vec4 = VEC && !trans;
   auto load_tile = [&](int c0, float (&pre)[32]) {
+    if (vec4) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = tid + 512 * i, w = e >> 5, j = e & 31;
+        const int a = 4 * (w >> 2) + (j >> 3), b = 32 * (w & 3) + 4 * (j & 7);
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r0 + a < n && c0 + b < n) {
+          // the row holds ldf >= n entries rounded up to four: the vector stays inside it
+          v = __ldg(reinterpret_cast<const float4*>(F + int64_t(r0 + a) * ldf + c0 + b));
+          if (c0 + b + 1 >= n) v.y = 0.f;
+          if (c0 + b + 2 >= n) v.z = 0.f;
+          if (c0 + b + 3 >= n) v.w = 0.f;
+        }
+        pre[4 * i] = v.x;
+        pre[4 * i + 1] = v.y;
+        pre[4 * i + 2] = v.z;
+        pre[4 * i + 3] = v.w;
+      }
+      return;
+    }
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
       const int e = tid + 512 * i;
@@ -1718,6 +1745,16 @@ __global__ void __launch_bounds__(512) trsv128_f32_kernel(const float* __restric
     }
   };
   auto store_tile = [&](const float (&pre)[32]) {
+    if (vec4) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = tid + 512 * i, w = e >> 5, j = e & 31;
+        const int a = 4 * (w >> 2) + (j >> 3), b = 32 * (w & 3) + 4 * (j & 7);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) sT[a][b + k] = pre[4 * i + k];
+      }
+      return;
+    }
 #pragma unroll
     for (int i = 0; i < 32; ++i) {
       const int e = tid + 512 * i;
@@ -1881,13 +1918,16 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
         return !(v && std::atoi(v) == 64);
       }();
       if (rows128 && dinv128) {
-        static std::atomic<unsigned long long> attr128[4] = {};
+        static std::atomic<unsigned long long> attr128[6] = {};
         int e;
         if ((e = smem_opt_in((const void*)trsv128_f32_kernel<0>, int(kTrsv128Smem), attr128[0])) ||
             (e = smem_opt_in((const void*)trsv128_f32_kernel<1>, int(kTrsv128Smem), attr128[1])) ||
             (e = smem_opt_in((const void*)trsv128_f32_kernel<2>, int(kTrsv128Smem), attr128[2])) ||
-            (e = smem_opt_in((const void*)trsv128_f32_kernel<3>, int(kTrsv128Smem), attr128[3])))
+            (e = smem_opt_in((const void*)trsv128_f32_kernel<3>, int(kTrsv128Smem), attr128[3])) ||
+            (e = smem_opt_in((const void*)trsv128_f32_kernel<0, true>, int(kTrsv128Smem), attr128[4])) ||
+            (e = smem_opt_in((const void*)trsv128_f32_kernel<1, true>, int(kTrsv128Smem), attr128[5])))
           return e;
+        const bool vec = (ldf & 3) == 0 && (reinterpret_cast<uintptr_t>(F) & 15) == 0;
         const unsigned g = unsigned(ceil_div(n, kTB2));
         // UPDES_TRSV_TAGS=0 hands solved blocks over by the finished-block count instead of tagged words
         static const bool tags_on = [] {
@@ -1897,8 +1937,14 @@ int trsv_impl(int n, const TF* F, int64_t ldf, double* x, int mode, int* sync_ws
         unsigned long long* tg = tags_on ? xtag : nullptr;
         if (tg) UPDES_CUDA_TRY(cudaMemsetAsync(tg, 0, 2 * size_t(n) * sizeof(unsigned long long), s));
         switch (mode) {
-          case 0: trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
-          case 1: trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
+          case 0:
+            if (vec) trsv128_f32_kernel<0, true><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg);
+            else trsv128_f32_kernel<0><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg);
+            break;
+          case 1:
+            if (vec) trsv128_f32_kernel<1, true><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg);
+            else trsv128_f32_kernel<1><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg);
+            break;
           case 2: trsv128_f32_kernel<2><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
           default: trsv128_f32_kernel<3><<<g, 512, kTrsv128Smem, s>>>(F, ldf, n, x, xh, xl, ticket, flags, st, dinv128, tg); break;
         }
