@@ -196,3 +196,35 @@ def test_support_size_edge_values():
         U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size=1)
     with pytest.raises(ValueError):
         U.SquareCloud(Nx=5, Ny=4, facet_types=facets, support_size=2.5)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_stacked_probes_equal_probes_one_by_one(name, monkeypatch):
+    """The eight capture probes evaluated in one stacked call give the same weights, bit for bit, as the
+    probes evaluated one at a time."""
+    from updes_gb300 import operators as OPS
+    g = load(name)
+    case = case_of(g)
+    cl = product_cloud(case)
+    X = cl.sorted_nodes[:cl.Ni]
+    fields = C.make_fields(case, cl.sorted_nodes)
+    fl = None if fields is None else fields[:, :cl.Ni]
+    op = _diff_operator(case["op"])
+    stacked = U.capture_operator(op, X, U.polyharmonic, fl)
+    monkeypatch.setattr(OPS, "_STACKED_PROBE_MAX_NODES", -1)
+    assert np.array_equal(stacked, U.capture_operator(op, X, U.polyharmonic, fl))
+
+
+def test_stacked_probe_falls_back_for_an_operator_that_mixes_probes(monkeypatch):
+    """An operator that reduces over a primitive's whole value (here the mean of nodal_value, which is the
+    value itself for one probe) mixes the stacked probes; the check against a separate evaluation catches it
+    and the probes run one by one, giving the one-by-one weights."""
+    from updes_gb300 import operators as OPS
+    X = np.random.default_rng(1).uniform(size=(9, 2))
+    op = lambda x, c, r, m, f: U.nodal_laplacian(x, c, r, m) + np.mean(U.nodal_value(x, c, r, m))
+    calls = []
+    orig = OPS.np.array_equal
+    monkeypatch.setattr(OPS.np, "array_equal", lambda a, b: calls.append(orig(a, b)) or calls[-1])
+    W = U.capture_operator(op, X, U.polyharmonic, None)
+    assert calls == [False]
+    assert np.allclose(W[:, 0], 1.0) and np.allclose(W[:, 1:3], 0.0) and np.allclose(W[:, 3:], 1.0)

@@ -119,6 +119,31 @@ def _align(k: int, unit: int) -> int:
     return (k + unit - 1) // unit * unit
 
 
+def _pack_layout(sizes):
+    """Offsets, in elements, of every system's arrays in the batch's packed buffers, each array starting on a
+    256-byte boundary (32 doubles, 64 ints).  ``sizes``: (N, Ni, n) per system.  Returns (f64 offsets of nodes
+    (2N), operator weights (5 Ni), boundary geometry (8 Nb) and q (N); int32 offsets of boundary kinds (Nb) and
+    node pairs (2 Nb); output offsets of coefficients (n) and values (N); the three buffers' lengths)."""
+    f_off, i_off, o_off = [], [], []
+    fpos = ipos = opos = 0
+    for N, Ni, n in sizes:
+        Nb = N - Ni
+        offs = []
+        for sz in (2 * N, 5 * Ni, 8 * Nb, N):
+            offs.append(fpos)
+            fpos = _align(fpos + sz, 32)
+        f_off.append(offs)
+        kinds = ipos
+        pairs = _align(kinds + Nb, 64)
+        i_off.append((kinds, pairs))
+        ipos = _align(pairs + 2 * Nb, 64)
+        co = opos
+        vo = _align(co + n, 32)
+        o_off.append((co, vo))
+        opos = _align(vo + N, 32)
+    return f_off, i_off, o_off, (fpos, ipos, opos)
+
+
 class _PackedProblem:
     """One system of a batch: sizes, kernel and the ``updes_problem`` struct, whose arrays live in the batch's
     packed device buffers (the object keeps them alive)."""
@@ -148,22 +173,8 @@ class _Batch:
         dev = torch.device("cuda", torch.cuda.current_device())
         c = len(prepared)
         self.count = c
-        # offsets (in elements) of each system's arrays: 32 doubles / 64 ints = 256 bytes
-        f_off, i_off, o_off = [], [], []
-        fpos = ipos = opos = 0
-        for cl, (W, kind, bnodes, geom, q), deg in zip(clouds, prepared, degrees):
-            N, Ni, Nb = cl.N, cl.Ni, cl.N - cl.Ni
-            n = N + compute_nb_monomials(deg)
-            sizes = (2 * N, 5 * Ni, 8 * Nb, N)  # nodes, op weights, boundary geometry, q
-            offs = []
-            for sz in sizes:
-                offs.append(fpos)
-                fpos = _align(fpos + sz, 32)
-            f_off.append(offs)
-            i_off.append((ipos, _align(ipos + Nb, 64)))  # boundary kinds, boundary node pairs
-            ipos = _align(i_off[-1][1] + 2 * Nb, 64)
-            o_off.append((opos, _align(opos + n, 32)))  # coefficients, values
-            opos = _align(o_off[-1][1] + N, 32)
+        f_off, i_off, o_off, (fpos, ipos, opos) = _pack_layout(
+            [(cl.N, cl.Ni, cl.N + compute_nb_monomials(deg)) for cl, deg in zip(clouds, degrees)])
         fh = np.zeros(max(fpos, 1), dtype=np.float64)
         ih = np.zeros(max(ipos, 1), dtype=np.int32)
         for cl, (W, kind, bnodes, geom, q), fo, io in zip(clouds, prepared, f_off, i_off):
