@@ -260,6 +260,7 @@ FIELD_INTEGRAL_CASES = {
 FIELD_INTERP_CASE = dict(Nx=8, Ny=8, facets1=dict(South="n", West="d", North="n", East="d"),
                          facets2=dict(South="d", West="n", North="d", East="n"))
 FIELD_FD_CASE = dict(Nx=9, Ny=7, facets=dict(North="n", South="n", East="d", West="n"), jitter=(0.15, 7))
+FIELD_FD_SUPPORT = 12  # the grid finite differences again on 12-nearest-node supports
 FIELD_EVAL_POINTS = np.array([[0.31, 0.42], [0.5, 0.5], [0.05, 0.9], [0.77, 0.13], [1.0, 0.25], [0.0, 0.0],
                               [0.62, 0.99]])
 

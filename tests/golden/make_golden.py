@@ -351,6 +351,12 @@ def run_fields(updes):
     grads = updes.cartesian_gradient_vec(range(cloud.N), jnp.asarray(f), cloud)
     out["fd_cartesian_gradient"] = npy(grads)
     out["fd_enforced"] = npy(updes.enforce_cartesian_gradient_neumann(jnp.asarray(f), grads, bcs, cloud))
+    # the same on k-nearest supports (support_size an int)
+    cloud = injected(fd["Nx"], fd["Ny"], fd["facets"], coords, support=C.FIELD_FD_SUPPORT)
+    out["fdl_neumann"] = npy(updes.apply_neumann_conditions(jnp.asarray(f), bcs, cloud))
+    grads = updes.cartesian_gradient_vec(range(cloud.N), jnp.asarray(f), cloud)
+    out["fdl_cartesian_gradient"] = npy(grads)
+    out["fdl_enforced"] = npy(updes.enforce_cartesian_gradient_neumann(jnp.asarray(f), grads, bcs, cloud))
     np.savez_compressed(os.path.join(HERE, "fields_helpers.npz"), **out)
     print(f"fields_helpers: {len(out)} arrays, {time.time() - t0:.1f}s")
 

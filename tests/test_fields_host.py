@@ -77,3 +77,16 @@ def test_small_helpers():
     from updes_gb300.operators import _bc_values_and_betas
     _, robin_solver = _bc_values_and_betas(bcs, cl, True)
     assert robin_solver == robin
+
+
+def test_grid_finite_differences_on_local_supports_match_the_reference():
+    fd = C.FIELD_FD_CASE
+    cloud = SquareCloud(Nx=fd["Nx"], Ny=fd["Ny"], facet_types=dict(fd["facets"]), coords=C.grid_coords(fd),
+                        support_size=C.FIELD_FD_SUPPORT)
+    f = GOLD["fd_field"]
+    bcs = {k: None for k in fd["facets"]}
+    assert np.allclose(F.apply_neumann_conditions(f, bcs, cloud), GOLD["fdl_neumann"], rtol=0, atol=1e-15)
+    grads = F.cartesian_gradient_vec(range(cloud.N), f, cloud)
+    assert np.allclose(grads, GOLD["fdl_cartesian_gradient"], rtol=1e-13, atol=1e-13)
+    assert np.allclose(F.enforce_cartesian_gradient_neumann(f, grads, bcs, cloud), GOLD["fdl_enforced"],
+                       rtol=1e-13, atol=1e-13)
