@@ -12,6 +12,8 @@ int ozaki_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t ld
 // (ozaki3_scratch_bytes(m, nc, K) bytes, 256-byte aligned), 8 digit products, TMA-fed.  The kernel keeps one
 // CTA per SM; `max_ctas` > 0 caps its grid so that work on another stream keeps the remaining SMs.
 size_t ozaki3_scratch_bytes(int mmax, int ncmax, int Kmax);
+// a_digits_ready: the previous update on `scratch` had the same A (same m, K and values), whose digits and
+// scales are still there; only B's are written.
 int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
                   int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s,
-                  int max_ctas = 0);
+                  int max_ctas = 0, bool a_digits_ready = false);

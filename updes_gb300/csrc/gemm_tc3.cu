@@ -661,7 +661,7 @@ size_t ozaki3_scratch_bytes(int mmax, int ncmax, int Kmax) {
 
 int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t lda, const float* B, int64_t ldb,
                   int m, int nc, int K, void* scratch, size_t scratch_bytes, DeviceStatus* st, cudaStream_t s,
-                  int max_ctas) {
+                  int max_ctas, bool a_digits_ready) {
   if (m <= 0 || nc <= 0 || K <= 0) return UPDES_OK;
   // the tile accumulator's low word is left unnormalised across k blocks: a few blocks only
   if (K > 1024) return UPDES_ERR_UNSUPPORTED;
@@ -672,13 +672,14 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
     return UPDES_ERR_UNSUPPORTED;
   const int Kp = int(ceil_div(K, TK)) * TK, nkb = Kp / TK;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+  // A's digits and scales first: their place depends only on m and K, so an update with the same A can reuse them
   char* p = static_cast<char*>(scratch);
   __nv_bfloat16* Ad = reinterpret_cast<__nv_bfloat16*>(p);
   p += al(kDigits * size_t(m) * Kp * 2);
-  __nv_bfloat16* Bd = reinterpret_cast<__nv_bfloat16*>(p);
-  p += al(kDigits * size_t(nc) * Kp * 2);
   float* As = reinterpret_cast<float*>(p);
   p += al(size_t(m) * nkb * 4);
+  __nv_bfloat16* Bd = reinterpret_cast<__nv_bfloat16*>(p);
+  p += al(kDigits * size_t(nc) * Kp * 2);
   float* Bs = reinterpret_cast<float*>(p);
 
   static std::atomic<unsigned long long> attr{0};
@@ -693,7 +694,7 @@ int ozaki3_update(float* Chi, float* Clo, int64_t ldc, const float* A, int64_t l
   StatScope sc(kStatGemm, s, 2.0 * m * double(nc) * K, double(m) * nc * 16.0 + (double(m) + nc) * K * 4.0);
   {
     const int64_t warps = int64_t(m) * nkb;
-    const int row_blocks = int(ceil_div(warps * 32, 256)), col_tiles = int(ceil_div(nc, TN));
+    const int row_blocks = a_digits_ready ? 0 : int(ceil_div(warps * 32, 256)), col_tiles = int(ceil_div(nc, TN));
     digits_kernel<<<unsigned(row_blocks + col_tiles * nkb), 256, 0, s>>>(A, lda, m, B, ldb, nc, K, Kp, row_blocks,
                                                                       col_tiles, Ad, As, Bd, Bs);
     UPDES_LAUNCH_CHECK();

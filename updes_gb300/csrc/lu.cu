@@ -969,12 +969,22 @@ int lu_factor_df(int n, float* Whi, float* Wlo, int64_t ld, int32_t* piv, void* 
     return UPDES_OK;
   };
   // W[r0:r1, c0:c1] -= F[r0:r1, kk0:kk1] * F[kk0:kk1, c0:c1] on stream us with digit scratch dg, at most ctas CTAs
+  // The digits of the last A written into each scratch (the update after a block writes them for the next
+  // block's columns, and the rest of the trailing matrix has the same A: the block's L rows below it, which
+  // nothing changes in between; any other update on that scratch replaces them).
+  struct ADigits {
+    const void* dg = nullptr;
+    int r0 = -1, r1 = -1, kk0 = -1, kk1 = -1;
+  } a_main, a_side;
   auto upd = [&](int r0, int r1, int c0, int c1, int kk0, int kk1, cudaStream_t us, void* dg, size_t dgb,
                  int ctas) -> int {
     if (!use_v2) {
+      ADigits& last = (dg == digits) ? a_main : a_side;
+      const bool a_ready = last.dg == dg && last.r0 == r0 && last.r1 == r1 && last.kk0 == kk0 && last.kk1 == kk1;
       const int e3 = ozaki3_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld,
                                    Whi + int64_t(r0) * ld + kk0, ld, Whi + int64_t(kk0) * ld + c0, ld, r1 - r0,
-                                   c1 - c0, kk1 - kk0, dg, dgb, st, us, ctas);
+                                   c1 - c0, kk1 - kk0, dg, dgb, st, us, ctas, a_ready);
+      last = e3 == UPDES_OK ? ADigits{dg, r0, r1, kk0, kk1} : ADigits{};
       if (e3 != UPDES_ERR_UNSUPPORTED) return e3;
     }
     return ozaki_update(Whi + int64_t(r0) * ld + c0, Wlo + int64_t(r0) * ld + c0, ld, Whi + int64_t(r0) * ld + kk0,
