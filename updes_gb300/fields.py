@@ -126,6 +126,8 @@ def apply_neumann_conditions(field, boundary_conditions, cloud):
             continue
         for i in cloud.facet_nodes[f]:
             j, _, _ = _opposite_closest(cloud, i, cloud.outward_normals[i])
+            if j is None:
+                raise ValueError(f"Neumann node {i}: no support node lies opposite its outward normal")
             out[i] = out[j]
     return out
 
@@ -169,6 +171,8 @@ def enforce_cartesian_gradient_neumann(field, grads, boundary_conditions, cloud,
             continue
         for i in cloud.facet_nodes[f]:
             j, dist, _ = _opposite_closest(cloud, i, cloud.outward_normals[i])
+            if j is None:
+                raise ValueError(f"Neumann node {i}: no support node lies opposite its outward normal")
             out[i] = (field[i] - field[j]) / dist
     return np.clip(out, -clip_val, clip_val) if clip_val else out
 
