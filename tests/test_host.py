@@ -228,3 +228,14 @@ def test_stacked_probe_falls_back_for_an_operator_that_mixes_probes(monkeypatch)
     W = U.capture_operator(op, X, U.polyharmonic, None)
     assert calls == [False]
     assert np.allclose(W[:, 0], 1.0) and np.allclose(W[:, 1:3], 0.0) and np.allclose(W[:, 3:], 1.0)
+
+
+def test_kernel_forms_of_r():
+    from updes_gb300 import assembly as ASM
+    r = np.array([0.0, 0.5, 2.0])
+    assert np.allclose(ASM.polyharmonic_func(r, 1), r ** 3)
+    assert np.allclose(ASM.gaussian_func(r, 2.0), np.exp(-(2.0 * r) ** 2))
+    assert np.allclose(ASM.multiquadric_func(r, 1.5), np.sqrt(1 + (1.5 * r) ** 2))
+    assert np.allclose(ASM.inv_multiquadric_func(r, 1.5), 1 / np.sqrt(1 + (1.5 * r) ** 2))
+    assert np.allclose(ASM.thin_plate_func(r, 1), [0.0, np.log(0.5) * 0.25, np.log(2.0) * 4.0])
+    assert ASM.make_nodal_rbf(np.array([0.0, 0.0]), np.array([3.0, 4.0]), lambda d: 2 * d) == 10.0

@@ -13,6 +13,9 @@ from .operators import (
     nodal_div_grad, nodal_gradient, nodal_laplacian, nodal_value, pde_multi_solver, pde_solver, pde_solver_jit,
     pde_solver_many, pde_solver_jit_with_bc, value, value_vec,
 )
+from .assembly import (assemble_A, assemble_B, assemble_bd_Phi_P, assemble_invert_A, assemble_op_Phi_P, assemble_P,
+                       assemble_Phi, assemble_q, gaussian_func, inv_multiquadric_func, make_nodal_rbf,
+                       multiquadric_func, polyharmonic_func, thin_plate_func)
 from .batched import PanelTuner, pde_solver_batched
 from .fields import (apply_neumann_conditions, cartesian_gradient, cartesian_gradient_vec, divergence_vec, dot_mat,
                      dot_vec, duplicate_robin_coeffs, enforce_cartesian_gradient_neumann, gradient_vals,
