@@ -239,3 +239,32 @@ def test_kernel_forms_of_r():
     assert np.allclose(ASM.inv_multiquadric_func(r, 1.5), 1 / np.sqrt(1 + (1.5 * r) ** 2))
     assert np.allclose(ASM.thin_plate_func(r, 1), [0.0, np.log(0.5) * 0.25, np.log(2.0) * 4.0])
     assert ASM.make_nodal_rbf(np.array([0.0, 0.0]), np.array([3.0, 4.0]), lambda d: 2 * d) == 10.0
+
+
+@pytest.mark.parametrize("kind,param", [("polyharmonic", 1), ("polyharmonic", 2), ("gaussian", 1.7),
+                                        ("multiquadric", 0.8), ("inverse_multiquadric", 1.3), ("thin_plate", 1)])
+def test_core_derivatives_match_central_differences(kind, param):
+    """core_gradient_rbf / core_laplacian_rbf (the reference's grad and jacfwd(grad) of a kernel) against
+    central differences of the kernel itself; the monomial versions likewise."""
+    from functools import partial
+    rbf = {"polyharmonic": partial(U.polyharmonic, a=param), "gaussian": partial(U.gaussian, eps=param),
+           "multiquadric": partial(U.multiquadric, eps=param),
+           "inverse_multiquadric": partial(U.inverse_multiquadric, eps=param),
+           "thin_plate": partial(U.thin_plate, a=param)}[kind]
+    x, c, h = np.array([0.31, 0.72]), np.array([0.55, 0.41]), 1e-4
+    e = np.eye(2) * h
+    g = U.core_gradient_rbf(rbf)(x, c)
+    gfd = np.array([(rbf(x + e[i], c) - rbf(x - e[i], c)) / (2 * h) for i in range(2)])
+    assert np.allclose(g, gfd, rtol=1e-6, atol=1e-9)
+    H = U.core_laplacian_rbf(rbf)(x, c)
+    Hfd = np.array([[(U.core_gradient_rbf(rbf)(x + e[j], c)[i] - U.core_gradient_rbf(rbf)(x - e[j], c)[i]) /
+                     (2 * h) for j in range(2)] for i in range(2)])
+    assert np.allclose(H, Hfd, rtol=1e-6, atol=1e-8) and H[0, 1] == H[1, 0]
+    for mono in U.make_all_monomials(15):
+        gm = U.core_gradient_mon(mono)(x)
+        fd = np.array([(mono(x + e[i]) - mono(x - e[i])) / (2 * h) for i in range(2)])
+        assert np.allclose(gm, fd, rtol=1e-6, atol=1e-9)
+        Hm = U.core_laplacian_mon(mono)(x)
+        Hmfd = np.array([[(U.core_gradient_mon(mono)(x + e[j])[i] - U.core_gradient_mon(mono)(x - e[j])[i]) /
+                          (2 * h) for j in range(2)] for i in range(2)])
+        assert np.allclose(Hm, Hmfd, rtol=1e-6, atol=1e-8)

@@ -8,7 +8,8 @@ library built by ``updes_gb300/build.py`` (``python -c "import __graft_entry__ a
 from .cloud import Cloud, GmshCloud, SquareCloud
 from .operators import (
     DEFAULT_OPTIONS, LAST_INFO, CollocationMatrix, SolverOptions, SteadySol, boundary_conditions_func_to_arr,
-    capture_operator, compute_coefficients, compute_nb_monomials, core_compute_coefficients, divergence,
+    capture_operator, compute_coefficients, compute_nb_monomials, core_compute_coefficients, core_gradient_mon,
+    core_gradient_rbf, core_laplacian_mon, core_laplacian_rbf, divergence,
     get_field_coefficients, gradient, gradient_vec, laplacian, laplacian_vec, make_all_monomials, make_monomial,
     nodal_div_grad, nodal_gradient, nodal_laplacian, nodal_value, pde_multi_solver, pde_solver, pde_solver_jit,
     pde_solver_many, pde_solver_jit_with_bc, value, value_vec,

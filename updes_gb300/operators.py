@@ -154,6 +154,64 @@ def _rbf_terms_numeric(rbf, x, center):
     return phi, g1 * dx, g1 * dy, g1 + g2 * dx * dx, g1 + g2 * dy * dy
 
 
+def _rbf_hessian_offdiag(rbf, x, center):
+    """d2/dxdy of the kernel for one pair (closed form, radial: g2 dx dy), 0 at r = 0."""
+    from .rbf import KIND_NAMES
+    kid, p = rbf_spec(rbf)
+    dx, dy = np.asarray(x, dtype=np.float64) - np.asarray(center, dtype=np.float64)
+    r2 = dx * dx + dy * dy
+    if r2 == 0.0:
+        return 0.0
+    r = np.sqrt(r2)
+    kind = KIND_NAMES[kid]
+    if kind == "polyharmonic":
+        k = 2 * int(p) + 1
+        g2 = k * (k - 2) * r ** (k - 4)
+    elif kind == "gaussian":
+        g2 = 4 * p ** 4 * np.exp(-p * p * r2)
+    elif kind == "multiquadric":
+        g2 = -p ** 4 / np.sqrt(1 + p * p * r2) ** 3
+    elif kind == "inverse_multiquadric":
+        g2 = 3 * p ** 4 / np.sqrt(1 + p * p * r2) ** 5
+    else:
+        a = int(p)
+        g2 = r ** (2 * a - 4) * (2 * a * (2 * a - 2) * np.log(r) + 4 * a - 2)
+    return g2 * dx * dy
+
+
+def core_gradient_rbf(rbf):
+    """The kernel's gradient in x, as a function of (x, center) (updes/operators.py:34-35; closed form, 0
+    where the reference's automatic derivative is NaN, at x = center)."""
+    return lambda x, center: np.array(_rbf_terms_numeric(rbf, x, center)[1:3])
+
+
+def core_gradient_mon(monomial):
+    """The monomial's gradient, as a function of x (updes/operators.py:38-39)."""
+    return lambda x: np.array(_monomial_terms(monomial, x)[1:3])
+
+
+def core_laplacian_rbf(rbf):
+    """The kernel's Hessian in x (2 x 2), as a function of (x, center): the reference's
+    jacfwd(grad(rbf)), whose trace nodal_laplacian takes (updes/operators.py:63-65)."""
+    def hess(x, center):
+        t = _rbf_terms_numeric(rbf, x, center)
+        h = _rbf_hessian_offdiag(rbf, x, center)
+        return np.array([[t[3], h], [h, t[4]]])
+    return hess
+
+
+def core_laplacian_mon(monomial):
+    """The monomial's Hessian (2 x 2), as a function of x (updes/operators.py:67-69)."""
+    def hess(x):
+        t = _monomial_terms(monomial, x)
+        px, py = _MONO_EXP[getattr(monomial, "keywords", {}).get("id", 0)] if hasattr(monomial, "keywords") \
+            else (0, 0)
+        x0, x1 = float(x[0]), float(x[1])
+        h = px * py * x0 ** (px - 1) * x1 ** (py - 1) if px and py else 0.0
+        return np.array([[t[3], h], [h, t[4]]])
+    return hess
+
+
 def nodal_value(x, center=None, rbf=None, monomial=None):
     """RBF or monomial value at x (updes/operators.py:15-32)."""
     pr = getattr(_PROBE, "state", None)
