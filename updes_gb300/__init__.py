@@ -24,4 +24,8 @@ from .fields import (apply_neumann_conditions, cartesian_gradient, cartesian_gra
                      zerofy_periodic_cond)
 from .rbf import distance, gaussian, inverse_multiquadric, multiquadric, polyharmonic, rbf_spec, thin_plate
 
+# the reference's names of its un-jitted vmaps (updes/operators.py:149, 186, 207, 370)
+value_vec_, gradient_vec_, gradient_vals_vec_, laplacian_vals_vec_ = (value_vec, gradient_vec, gradient_vals_vec,
+                                                                      laplacian_vals_vec)
+
 __version__ = "0.1.0"
